@@ -1,0 +1,107 @@
+"""ctypes binding of libbcx.so (the C ABI declared in include/bcx.h).
+
+Loading fails loudly: if the shared library is missing or does not export an
+entry point, importing this module raises instead of falling back to anything.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libbcx.so"
+
+# status codes (include/bcx.h)
+SUCCESS = 0
+DEVICE_NOT_FOUND = -1
+MEM_ALLOCATION_FAILURE = -4
+OUT_OF_RESOURCES = -5
+BUILD_PROGRAM_FAILURE = -11
+INVALID_VALUE = -30
+INVALID_KERNEL_NAME = -46
+INVALID_BUFFER_SIZE = -61
+DEVICE_TIMEOUT = -9001
+UNSUPPORTED = -9002
+
+DTYPES = {"char": 0, "uchar": 1, "short": 2, "ushort": 3, "int": 4, "uint": 5, "long": 6,
+          "ulong": 7, "float": 8, "double": 9}
+DTYPE_SIZE = {"char": 1, "uchar": 1, "short": 2, "ushort": 2, "int": 4, "uint": 4, "long": 8,
+              "ulong": 8, "float": 4, "double": 8}
+OPS = {"plus": 0, "multiplies": 1, "min": 2, "max": 3, "bit_and": 4, "bit_or": 5, "bit_xor": 6,
+       "minus": 7, "divides": 8, "modulus": 9}
+UNARY_OPS = {"identity": 0, "negate": 1, "abs": 2, "sqrt": 3, "logical_not": 4, "bit_not": 5}
+
+_vp = C.c_void_p
+_sz = C.c_size_t
+_i = C.c_int
+_szp = C.POINTER(C.c_size_t)
+
+# name -> (restype, argtypes); the exported surface of include/bcx.h
+SIGNATURES = {
+    "bcx_get_version": (_i, [C.POINTER(_i)]),
+    "bcx_last_error_string": (C.c_char_p, []),
+    "bcx_device_count": (_i, [C.POINTER(_i)]),
+    "bcx_set_device": (_i, [_i]),
+    "bcx_device_info": (_i, [_i, C.c_char_p, _sz, C.POINTER(_i), _szp]),
+    "bcx_stream_create": (_i, [C.POINTER(_vp)]),
+    "bcx_stream_destroy": (_i, [_vp]),
+    "bcx_stream_synchronize": (_i, [_vp]),
+    "bcx_malloc": (_i, [C.POINTER(_vp), _sz]),
+    "bcx_free": (_i, [_vp]),
+    "bcx_malloc_host": (_i, [C.POINTER(_vp), _sz]),
+    "bcx_free_host": (_i, [_vp]),
+    "bcx_memcpy_async": (_i, [_vp, _vp, _sz, _vp]),
+    "bcx_memset_async": (_i, [_vp, _i, _sz, _vp]),
+    "bcx_device_error_check": (_i, [_vp]),
+    "bcx_radix_sort_keys": (_i, [_vp, _i, _vp, _sz, _i, _vp, _szp]),
+    "bcx_radix_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _i, _vp, _szp]),
+    "bcx_sort_keys": (_i, [_vp, _i, _vp, _sz, _i, _vp, _szp]),
+    "bcx_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _i, _vp, _szp]),
+    "bcx_sort_pairs_host": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _i]),
+    "bcx_scan": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _sz, _i, _vp, _szp]),
+    "bcx_reduce": (_i, [_vp, _i, _i, _vp, _sz, _vp, _i, _vp, _szp]),
+    "bcx_accumulate": (_i, [_vp, _i, _i, _vp, _sz, _vp, _vp, _i, _vp, _szp]),
+    "bcx_transform_unary": (_i, [_vp, _i, _i, _vp, _vp, _sz]),
+    "bcx_transform_binary": (_i, [_vp, _i, _i, _vp, _vp, _vp, _sz]),
+    "bcx_transform_saxpy": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _sz]),
+    "bcx_profile_enable": (_i, [_i]),
+    "bcx_profile_reset": (_i, []),
+    "bcx_profile_read": (_i, [C.c_char_p, _sz, C.POINTER(C.c_uint64), C.POINTER(C.c_double), _sz, _szp]),
+}
+
+
+class BcxError(RuntimeError):
+    """A libbcx call returned a non-zero status (an OpenCL-style cl_int code)."""
+
+    def __init__(self, status: int, where: str, text: str):
+        super().__init__(f"{where} failed with status {status}: {text}")
+        self.status = status
+
+
+def load(path: Path | None = None) -> C.CDLL:
+    p = Path(path or os.environ.get("BCX_LIBRARY", LIB_PATH))
+    if not p.exists():
+        raise ImportError(f"libbcx.so not found at {p}: build it with "
+                          "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)  # AttributeError if the symbol is missing
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_LIB: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        _LIB = load()
+    return _LIB
+
+
+def check(status: int, where: str) -> None:
+    if status != SUCCESS:
+        text = lib().bcx_last_error_string().decode(errors="replace")
+        raise BcxError(status, where, text)

@@ -1,0 +1,476 @@
+// bcx_scan.cu -- exclusive_scan / inclusive_scan as ONE pass over HBM.
+//
+// Reference: detail::scan_on_gpu (algorithm/detail/scan_on_gpu.hpp:187-324):
+// a 256-wide Hillis-Steele scan per work-group in local memory, a recursive
+// scan of the block sums, then a uniform-add pass (about three global passes,
+// ~12 launches at 2^30).  Exclusive output[0] = init (:59-66); in-place scans
+// go through a temporary copy (:281-308).
+//
+// GB300 design: single-pass decoupled look-back.  Each 256-thread block takes
+// the next tile from an atomic ticket (so a block only ever waits on tiles
+// that were handed out before it, which guarantees forward progress), streams
+// its tile with 16-byte loads (warp w owns a contiguous 32*V-vector run; in
+// chunk j lane l owns vector j*32 + l, so every load and store is fully
+// coalesced), scans in registers and warp shuffles, publishes its aggregate,
+// and warp 0 looks back over 32 predecessors at a time for the nearest
+// inclusive prefix.  In-place scans need no copy: a tile reads all of its input
+// before writing any output.  Inputs that fit one tile run as one launch with
+// no look-back.  Every wait on a predecessor is bounded (kSpinLimit polls); on
+// expiry the block records BCX_DEVICE_TIMEOUT and continues.
+//
+// Float plus with compensated=1 keeps Neumaier (s, c) pairs for every sum
+// inside a tile and carries tile prefixes between blocks in FP64.
+#include <cuda_runtime.h>
+
+#include <string.h>
+
+#include "bcx.h"
+#include "bcx_common.cuh"
+#include "bcx_internal.h"
+
+namespace bcx {
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanWarps = kScanThreads / kWarp;
+
+enum : uint32_t { kFlagInvalid = 0, kFlagAggregate = 1, kFlagPrefix = 2 };
+
+// ---- policies --------------------------------------------------------------
+template <class T, template <class> class OpT>
+struct ScanPlain {
+  typedef typename widen<T>::type Acc;
+  typedef Acc Carry;
+  typedef OpT<Acc> Op;
+  __device__ __forceinline__ static Acc ident() { return Op::identity(); }
+  __device__ __forceinline__ static Acc add(Acc a, T x) { return Op()(a, Acc(x)); }
+  __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return Op()(a, b); }
+  __device__ __forceinline__ static Carry to_carry(Acc a) { return a; }
+  __device__ __forceinline__ static Acc from_carry(Carry c) { return c; }
+  __device__ __forceinline__ static Carry carry_comb(Carry a, Carry b) { return Op()(a, b); }
+  __device__ __forceinline__ static Carry carry_ident() { return Op::identity(); }
+  __device__ __forceinline__ static T out(Acc a) { return T(a); }
+  __device__ __forceinline__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static Acc shfl(Acc a, int src) { return __shfl_sync(0xffffffffu, a, src); }
+  __device__ __forceinline__ static Carry carry_shfl_down(Carry a, int d) {
+    return __shfl_down_sync(0xffffffffu, a, d);
+  }
+  __device__ __forceinline__ static Carry carry_bcast(Carry a) { return __shfl_sync(0xffffffffu, a, 0); }
+  static Carry host_carry(const void *init) {
+    T v;
+    memcpy(&v, init, sizeof(T));
+    return Carry(v);
+  }
+};
+
+struct ScanCompF32 {
+  typedef comp_f32 Acc;
+  typedef double Carry;
+  __device__ __forceinline__ static Acc ident() { return comp_f32{0.f, 0.f}; }
+  __device__ __forceinline__ static Acc add(Acc a, float x) { return comp_add(a, x); }
+  __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return comp_merge(a, b); }
+  __device__ __forceinline__ static Carry to_carry(Acc a) { return double(a.s) + double(a.c); }
+  __device__ __forceinline__ static Acc from_carry(Carry c) {
+    float hi = float(c);
+    return comp_f32{hi, float(c - double(hi))};
+  }
+  __device__ __forceinline__ static Carry carry_comb(Carry a, Carry b) { return a + b; }
+  __device__ __forceinline__ static Carry carry_ident() { return 0.0; }
+  __device__ __forceinline__ static float out(Acc a) { return a.s + a.c; }
+  __device__ __forceinline__ static Acc shfl_up(Acc a, int d) {
+    return comp_f32{__shfl_up_sync(0xffffffffu, a.s, d), __shfl_up_sync(0xffffffffu, a.c, d)};
+  }
+  __device__ __forceinline__ static Acc shfl(Acc a, int src) {
+    return comp_f32{__shfl_sync(0xffffffffu, a.s, src), __shfl_sync(0xffffffffu, a.c, src)};
+  }
+  __device__ __forceinline__ static Carry carry_shfl_down(Carry a, int d) {
+    return __shfl_down_sync(0xffffffffu, a, d);
+  }
+  __device__ __forceinline__ static Carry carry_bcast(Carry a) { return __shfl_sync(0xffffffffu, a, 0); }
+  static Carry host_carry(const void *init) {
+    float v;
+    memcpy(&v, init, sizeof(float));
+    return double(v);
+  }
+};
+
+struct ScanCompF64 {
+  typedef comp_f64 Acc;
+  typedef comp_f64 Carry;
+  __device__ __forceinline__ static Acc ident() { return comp_f64{0.0, 0.0}; }
+  __device__ __forceinline__ static Acc add(Acc a, double x) { return comp_add(a, x); }
+  __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return comp_merge(a, b); }
+  __device__ __forceinline__ static Carry to_carry(Acc a) { return a; }
+  __device__ __forceinline__ static Acc from_carry(Carry c) { return c; }
+  __device__ __forceinline__ static Carry carry_comb(Carry a, Carry b) { return comp_merge(a, b); }
+  __device__ __forceinline__ static Carry carry_ident() { return comp_f64{0.0, 0.0}; }
+  __device__ __forceinline__ static double out(Acc a) { return a.s + a.c; }
+  __device__ __forceinline__ static Acc shfl_up(Acc a, int d) {
+    return comp_f64{__shfl_up_sync(0xffffffffu, a.s, d), __shfl_up_sync(0xffffffffu, a.c, d)};
+  }
+  __device__ __forceinline__ static Acc shfl(Acc a, int src) {
+    return comp_f64{__shfl_sync(0xffffffffu, a.s, src), __shfl_sync(0xffffffffu, a.c, src)};
+  }
+  __device__ __forceinline__ static Carry carry_shfl_down(Carry a, int d) {
+    return comp_f64{__shfl_down_sync(0xffffffffu, a.s, d), __shfl_down_sync(0xffffffffu, a.c, d)};
+  }
+  __device__ __forceinline__ static Carry carry_bcast(Carry a) {
+    return comp_f64{__shfl_sync(0xffffffffu, a.s, 0), __shfl_sync(0xffffffffu, a.c, 0)};
+  }
+  static Carry host_carry(const void *init) {
+    double v;
+    memcpy(&v, init, sizeof(double));
+    return comp_f64{v, 0.0};
+  }
+};
+
+// L2-coherent payload loads (issued after an acquire of the flag word).
+__device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ long long ldcg(const long long *p) { return __ldcg(p); }
+__device__ __forceinline__ unsigned long long ldcg(const unsigned long long *p) { return __ldcg(p); }
+__device__ __forceinline__ comp_f64 ldcg(const comp_f64 *p) {
+  return comp_f64{__ldcg(&p->s), __ldcg(&p->c)};
+}
+
+// ---- tile status -----------------------------------------------------------
+// 4-byte carries are packed with their flag into one 64-bit word, published
+// and read as a single 64-bit access.  Wider carries use a flag word plus
+// separate aggregate/inclusive arrays ordered by release/acquire.
+template <class Carry, bool PACKED = (sizeof(Carry) == 4)>
+struct TileStatus;
+
+template <class Carry>
+struct TileStatus<Carry, true> {
+  unsigned long long *words;
+  static size_t bytes(size_t tiles) { return align256(tiles * 8); }
+  static size_t zero_bytes(size_t tiles) { return bytes(tiles); }
+  void bind(char *base, size_t) { words = reinterpret_cast<unsigned long long *>(base); }
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, Carry v) {
+    uint32_t bits;
+    memcpy(&bits, &v, 4);
+    unsigned long long w = (static_cast<unsigned long long>(bits) << 32) | flag;
+    st_release_u64(&words[t], w);
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, Carry *v) const {
+    unsigned long long w = ld_acquire_u64(&words[t]);
+    uint32_t bits = uint32_t(w >> 32);
+    memcpy(v, &bits, 4);
+    return uint32_t(w & 0xffffffffu);
+  }
+};
+
+template <class Carry>
+struct TileStatus<Carry, false> {
+  uint32_t *flags;
+  Carry *agg;
+  Carry *inc;
+  static size_t bytes(size_t tiles) {
+    return align256(tiles * 4) + 2 * align256(tiles * sizeof(Carry));
+  }
+  static size_t zero_bytes(size_t tiles) { return align256(tiles * 4); }
+  void bind(char *base, size_t tiles) {
+    flags = reinterpret_cast<uint32_t *>(base);
+    agg = reinterpret_cast<Carry *>(base + align256(tiles * 4));
+    inc = reinterpret_cast<Carry *>(base + align256(tiles * 4) + align256(tiles * sizeof(Carry)));
+  }
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, Carry v) {
+    if (flag == kFlagAggregate) agg[t] = v;
+    else inc[t] = v;
+    st_release_u32(&flags[t], flag);
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, Carry *v) const {
+    uint32_t f = ld_acquire_u32(&flags[t]);
+    if (f == kFlagAggregate) *v = ldcg(&agg[t]);
+    else if (f == kFlagPrefix) *v = ldcg(&inc[t]);
+    return f;
+  }
+};
+
+// Warp 0 of a block: publish this tile's aggregate, look back for the
+// exclusive prefix, publish the inclusive prefix.  Returns the exclusive
+// prefix (valid in every lane of warp 0).
+template <class P, class Status>
+__device__ __forceinline__ typename P::Carry lookback(Status &st, size_t tile,
+                                                      typename P::Carry agg, uint32_t *err) {
+  typedef typename P::Carry C;
+  const unsigned lane = lane_id();
+  if (lane == 0) st.publish(tile, kFlagAggregate, agg);
+  C excl = P::carry_ident();
+  long long pred = (long long)tile - 1;
+  bool gave_up = false;
+  while (true) {
+    long long t = pred - (long long)lane;
+    C v = P::carry_ident();
+    uint32_t f = kFlagPrefix;  // beyond tile 0: nothing to add
+    if (t >= 0) {
+      uint32_t spins = 0;
+      f = st.poll(size_t(t), &v);
+      while (f == kFlagInvalid) {
+        if (++spins > kSpinLimit) {
+          gave_up = true;
+          f = kFlagPrefix;
+          v = P::carry_ident();
+          break;
+        }
+        __nanosleep(spins < 64 ? 32 : 256);
+        f = st.poll(size_t(t), &v);
+      }
+    }
+    const unsigned pmask = __ballot_sync(0xffffffffu, f == kFlagPrefix);
+    const int first = pmask ? __ffs(pmask) - 1 : 31;
+    if (int(lane) > first) v = P::carry_ident();
+    // Lane 0 folds lanes 0..first: the window of predecessors nearest to this
+    // tile, ending at the nearest inclusive prefix.
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+      C o = P::carry_shfl_down(v, d);
+      if (int(lane) + d < kWarp) v = P::carry_comb(v, o);
+    }
+    const C window = P::carry_bcast(v);
+    excl = P::carry_comb(window, excl);
+    if (pmask) break;
+    pred -= 32;
+  }
+  if (__any_sync(0xffffffffu, gave_up) && lane == 0) report_error(err, kErrLookbackTimeout);
+  if (lane == 0) st.publish(tile, kFlagPrefix, P::carry_comb(excl, agg));
+  return excl;
+}
+
+template <class T>
+__device__ __forceinline__ void load_chunk(const T *__restrict__ in, size_t vi, size_t head_pad,
+                                           size_t nv, bool vec_ok, T (&x)[16 / sizeof(T)],
+                                           bool (&valid)[16 / sizeof(T)]) {
+  constexpr int N = 16 / sizeof(T);
+  const size_t u0 = vi * N;
+  if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
+    vec16<T> r = ld_stream16(reinterpret_cast<const vec16<T> *>(in - head_pad) + vi);
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      x[k] = r.v[k];
+      valid[k] = true;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const size_t u = u0 + k;
+      valid[k] = (u >= head_pad && u < nv);
+      x[k] = valid[k] ? in[u - head_pad] : T(0);
+    }
+  }
+}
+
+// One block = one tile of kScanThreads * V vectors.
+template <class T, class P, int V, bool SINGLE, class Status>
+__global__ void __launch_bounds__(kScanThreads)
+scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t head_pad,
+                 int vec_ok, int exclusive, typename P::Carry init_carry, Status st,
+                 uint32_t *tile_counter, uint32_t *err) {
+  typedef typename P::Acc Acc;
+  typedef typename P::Carry Carry;
+  constexpr int N = 16 / sizeof(T);
+  __shared__ Acc warp_tot[kScanWarps];
+  __shared__ Carry tile_prefix;
+  __shared__ uint32_t tile_slot;
+
+  const unsigned lane = lane_id();
+  const unsigned warp = threadIdx.x / kWarp;
+  size_t tile = 0;
+  if (!SINGLE) {
+    if (threadIdx.x == 0) tile_slot = atomicAdd(tile_counter, 1u);
+    __syncthreads();
+    tile = tile_slot;
+  }
+  const size_t nv = n + head_pad;
+  const size_t tile_vec0 = tile * size_t(kScanThreads) * V;
+  const size_t warp_vec0 = tile_vec0 + size_t(warp) * kWarp * V;
+
+  T x[V][N];
+  bool valid[V][N];
+  Acc lane_excl[V];
+  Acc chunk_pre[V];
+  Acc run = P::ident();
+#pragma unroll
+  for (int j = 0; j < V; ++j) load_chunk<T>(in, warp_vec0 + size_t(j) * kWarp + lane, head_pad, nv, vec_ok != 0, x[j], valid[j]);
+#pragma unroll
+  for (int j = 0; j < V; ++j) {
+    Acc t = P::ident();
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      if (valid[j][k]) t = P::add(t, x[j][k]);
+    // inclusive warp scan of the per-lane totals of chunk j
+    Acc incl = t;
+#pragma unroll
+    for (int d = 1; d < kWarp; d <<= 1) {
+      Acc o = P::shfl_up(incl, d);
+      if (int(lane) >= d) incl = P::comb(o, incl);
+    }
+    Acc ex = P::shfl_up(incl, 1);
+    lane_excl[j] = (lane == 0) ? P::ident() : ex;
+    chunk_pre[j] = run;
+    run = P::comb(run, P::shfl(incl, kWarp - 1));
+  }
+  if (lane == 0) warp_tot[warp] = run;
+  __syncthreads();
+  Acc warp_excl = P::ident();
+  Acc tile_agg = P::ident();
+#pragma unroll
+  for (int w = 0; w < kScanWarps; ++w) {
+    if (w == int(warp)) warp_excl = tile_agg;
+    tile_agg = P::comb(tile_agg, warp_tot[w]);
+  }
+  if (SINGLE) {
+    if (threadIdx.x == 0) tile_prefix = init_carry;
+  } else if (warp == 0) {
+    Carry pre;
+    if (tile == 0) {
+      pre = init_carry;
+      if (lane == 0) st.publish(0, kFlagPrefix, P::carry_comb(init_carry, P::to_carry(tile_agg)));
+    } else {
+      pre = lookback<P>(st, tile, P::to_carry(tile_agg), err);
+    }
+    if (lane == 0) tile_prefix = pre;
+  }
+  __syncthreads();
+  const Acc base = P::comb(P::from_carry(tile_prefix), warp_excl);
+  T *vout_base = out - head_pad;
+#pragma unroll
+  for (int j = 0; j < V; ++j) {
+    Acc r = P::comb(P::comb(base, chunk_pre[j]), lane_excl[j]);
+    T y[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      if (exclusive) {
+        y[k] = P::out(r);
+        if (valid[j][k]) r = P::add(r, x[j][k]);
+      } else {
+        if (valid[j][k]) r = P::add(r, x[j][k]);
+        y[k] = P::out(r);
+      }
+    }
+    const size_t vi = warp_vec0 + size_t(j) * kWarp + lane;
+    const size_t u0 = vi * N;
+    if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
+      vec16<T> w;
+#pragma unroll
+      for (int k = 0; k < N; ++k) w.v[k] = y[k];
+      st_stream16(reinterpret_cast<vec16<T> *>(vout_base) + vi, w);
+    } else {
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        if (valid[j][k]) vout_base[u0 + k] = y[k];
+    }
+  }
+}
+
+template <class T> struct scan_vectors_per_thread { static constexpr int value = 4; };
+
+template <class T, class P>
+bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const void *in, void *out,
+                      size_t n, void *temp, size_t *temp_bytes) {
+  typedef typename P::Carry Carry;
+  typedef TileStatus<Carry> Status;
+  constexpr int N = 16 / sizeof(T);
+  constexpr int V = scan_vectors_per_thread<T>::value;
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
+  const uintptr_t ain = reinterpret_cast<uintptr_t>(in), aout = reinterpret_cast<uintptr_t>(out);
+  const bool elem_aligned = (ain % sizeof(T) == 0) && (aout % sizeof(T) == 0);
+  const bool vec_ok = elem_aligned && ((ain & 15u) == (aout & 15u));
+  const size_t head_pad = vec_ok ? (ain & 15u) / sizeof(T) : 0;
+  const size_t nv = n + head_pad;
+  const size_t tile_elems = size_t(kScanThreads) * V * N;
+  const size_t tiles = div_up(nv, tile_elems);
+  const bool single = (tiles <= 1);
+  const size_t need = single ? 0 : (256 + Status::bytes(tiles));
+  TempStorage ts;
+  bool query = false;
+  rc = ts.acquire(temp, temp_bytes, need, s, &query);
+  if (rc || query) return rc;
+  Carry init_carry = P::host_carry(init);
+  const T *pin = static_cast<const T *>(in);
+  T *pout = static_cast<T *>(out);
+  if (single) {
+    Status st{};
+    KernelScope ks("scan_single", s);
+    scan_tile_kernel<T, P, V, true, Status><<<1, kScanThreads, 0, s>>>(
+        pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, nullptr, ds->err_word);
+    return launch_status("scan_single");
+  }
+  char *base = static_cast<char *>(ts.ptr());
+  uint32_t *counter = reinterpret_cast<uint32_t *>(base);
+  Status st;
+  st.bind(base + 256, tiles);
+  BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
+  BCX_CHECK(tiles < (size_t(1) << 31), BCX_INVALID_VALUE, "scan: input too large");
+  KernelScope ks("scan_lookback", s);
+  scan_tile_kernel<T, P, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
+      pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);
+  return launch_status("scan_lookback");
+}
+
+template <class T>
+bcx_status dispatch_int(cudaStream_t s, int op, int ex, const void *init, const void *in,
+                        void *out, size_t n, void *temp, size_t *tb) {
+  switch (op) {
+    case BCX_PLUS: return run_scan_t<T, ScanPlain<T, op_plus>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_MULTIPLIES: return run_scan_t<T, ScanPlain<T, op_multiplies>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_MIN: return run_scan_t<T, ScanPlain<T, op_min>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_MAX: return run_scan_t<T, ScanPlain<T, op_max>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_BIT_AND: return run_scan_t<T, ScanPlain<T, op_bit_and>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_BIT_OR: return run_scan_t<T, ScanPlain<T, op_bit_or>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_BIT_XOR: return run_scan_t<T, ScanPlain<T, op_bit_xor>>(s, ex, init, in, out, n, temp, tb);
+  }
+  return BCX_UNSUPPORTED;
+}
+
+template <class T>
+bcx_status dispatch_float(cudaStream_t s, int op, int ex, const void *init, const void *in,
+                          void *out, size_t n, int comp, void *temp, size_t *tb) {
+  switch (op) {
+    case BCX_PLUS:
+      if (comp) {
+        if (sizeof(T) == 4) return run_scan_t<float, ScanCompF32>(s, ex, init, in, out, n, temp, tb);
+        return run_scan_t<double, ScanCompF64>(s, ex, init, in, out, n, temp, tb);
+      }
+      return run_scan_t<T, ScanPlain<T, op_plus>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_MULTIPLIES: return run_scan_t<T, ScanPlain<T, op_multiplies>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_MIN: return run_scan_t<T, ScanPlain<T, op_min>>(s, ex, init, in, out, n, temp, tb);
+    case BCX_MAX: return run_scan_t<T, ScanPlain<T, op_max>>(s, ex, init, in, out, n, temp, tb);
+  }
+  return BCX_UNSUPPORTED;
+}
+
+}  // namespace
+}  // namespace bcx
+
+extern "C" bcx_status bcx_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive,
+                               const void *init, const void *in, void *out, size_t n,
+                               int compensated, void *temp, size_t *temp_bytes) {
+  using namespace bcx;
+  clear_error();
+  BCX_CHECK(dtype_valid(type), BCX_INVALID_VALUE, "invalid dtype %d", int(type));
+  if (n == 0) {
+    if (temp == nullptr && temp_bytes != nullptr) *temp_bytes = 0;
+    return BCX_SUCCESS;
+  }
+  BCX_CHECK(in != nullptr && out != nullptr, BCX_INVALID_VALUE, "NULL input or output");
+  unsigned char zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const void *init_p = (exclusive && init) ? init : zero;
+  cudaStream_t s = (cudaStream_t)stream;
+  bcx_status rc = BCX_UNSUPPORTED;
+  switch (type) {
+    case BCX_CHAR: rc = dispatch_int<int8_t>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_UCHAR: rc = dispatch_int<uint8_t>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_SHORT: rc = dispatch_int<int16_t>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_USHORT: rc = dispatch_int<uint16_t>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_INT: rc = dispatch_int<int32_t>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_UINT: rc = dispatch_int<uint32_t>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_LONG: rc = dispatch_int<long long>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_ULONG: rc = dispatch_int<unsigned long long>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
+    case BCX_FLOAT: rc = dispatch_float<float>(s, op, exclusive, init_p, in, out, n, compensated, temp, temp_bytes); break;
+    case BCX_DOUBLE: rc = dispatch_float<double>(s, op, exclusive, init_p, in, out, n, compensated, temp, temp_bytes); break;
+  }
+  if (rc == BCX_UNSUPPORTED) set_error("scan: functor %d not provided for dtype %d", int(op), int(type));
+  return rc;
+}

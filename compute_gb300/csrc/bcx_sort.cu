@@ -1,0 +1,631 @@
+// bcx_sort.cu -- sort / sort_by_key: onesweep LSD radix sort with 8-bit digits.
+//
+// Reference: detail::radix_sort_impl (algorithm/detail/radix_sort.hpp:253-426)
+// runs sizeof(T)*8/4 passes of 4-bit digits; each pass launches a count kernel
+// (per-group 16-bin histogram), an exclusive_scan of the block histograms,
+// a single work-item scan of the digit totals and a scatter kernel whose
+// work-items rank themselves with an O(block) serial loop (:235-239), ping-
+// ponging between the input and a temporary (:421-424).  Small inputs go to a
+// single work-item insertion sort (sort.hpp:34-80, insertion_sort.hpp:26-159).
+//
+// GB300 design (onesweep):
+//   1. one histogram kernel reads the keys once and builds the 256-bin digit
+//      histogram of EVERY pass in shared memory (warp-uniform digits are
+//      added once per warp instead of once per lane);
+//   2. a one-block prep kernel turns them into per-pass digit start offsets,
+//      marks passes whose digit is the same for all keys (an identity
+//      permutation: skipped, which keeps the result bit-identical), and
+//      decides which buffer each pass reads and writes;
+//   3. one kernel per 8-bit digit: each block takes the next tile from an
+//      atomic ticket, loads its keys (and values) warp-striped and fully
+//      coalesced, ranks them with __match_any_sync against per-warp digit
+//      counters in shared memory (stable: ranks follow input order), publishes
+//      its 256 digit counts, looks back over predecessor tiles per digit for
+//      the global offset (decoupled look-back, bounded waits), stages keys and
+//      values in shared memory in digit order and writes them out as runs of
+//      consecutive addresses;
+//   4. if an odd number of passes ran, one copy kernel moves the result back.
+// Every launch is asynchronous on the caller's stream; nothing reads back to
+// the host, so the whole sort can be captured in a CUDA graph.
+//
+// The digit of a key is taken from the reference's radix() transform
+// (bcx_common.cuh radix_key), so the order of equal-under-transform keys, of
+// -0.0/+0.0 and of NaNs is the reference's.
+#include <cuda_runtime.h>
+
+#include <string.h>
+
+#include "bcx.h"
+#include "bcx_common.cuh"
+#include "bcx_internal.h"
+
+namespace bcx {
+namespace {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / kWarp;
+constexpr int kHistThreads = 256;
+
+// Status word of one (tile, digit): 2-bit flag above a 30-bit count.
+constexpr uint32_t kStFlagShift = 30;
+constexpr uint32_t kStValueMask = (1u << kStFlagShift) - 1;
+constexpr uint32_t kStAggregate = 1u << kStFlagShift;
+constexpr uint32_t kStPrefix = 2u << kStFlagShift;
+constexpr size_t kMaxSortN = size_t(1) << 30;
+
+enum KeyKind : int { kKeyUnsigned = 0, kKeySigned = 1, kKeyFloat = 2 };
+
+template <class U>
+__device__ __forceinline__ U radix_key_rt(U x, int kind, int desc) {
+  if (kind == kKeyFloat) return desc ? radix_key<U, true, true, true>(x) : radix_key<U, true, true, false>(x);
+  if (kind == kKeySigned) return desc ? radix_key<U, false, true, true>(x) : radix_key<U, false, true, false>(x);
+  return desc ? radix_key<U, false, false, true>(x) : radix_key<U, false, false, false>(x);
+}
+
+template <int VB> struct value_type_of;
+template <> struct value_type_of<0> { typedef uint8_t type; };
+template <> struct value_type_of<1> { typedef uint8_t type; };
+template <> struct value_type_of<2> { typedef uint16_t type; };
+template <> struct value_type_of<4> { typedef uint32_t type; };
+template <> struct value_type_of<8> { typedef unsigned long long type; };
+template <> struct value_type_of<16> { typedef uint4 type; };
+
+template <class U> struct items_per_thread { static constexpr int value = 16; };
+template <> struct items_per_thread<unsigned long long> { static constexpr int value = 12; };
+
+// Device-side control block written by the prep kernel.
+struct SortControl {
+  uint32_t skip[8];     // pass p moves nothing (all keys share its digit)
+  uint32_t src_alt[8];  // pass p reads the temporary buffers
+  uint32_t final_alt;   // the sorted data ended in the temporary buffers
+  uint32_t pad[47];
+};
+static_assert(sizeof(SortControl) == 256, "control block is 256 bytes");
+
+// ---------------------------------------------------------------------------
+// 1. Histogram of every digit position, one read of the keys.
+template <class U, int PASSES>
+__global__ void __launch_bounds__(kHistThreads)
+radix_histogram_kernel(const U *__restrict__ keys, size_t n, int kind, int desc,
+                       uint32_t *__restrict__ hist) {
+  __shared__ uint32_t sh[PASSES][kRadix];
+  for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
+  __syncthreads();
+  const size_t gtid = size_t(blockIdx.x) * kHistThreads + threadIdx.x;
+  const size_t stride = size_t(gridDim.x) * kHistThreads;
+  const unsigned lane = lane_id();
+  // Every lane of a warp runs the same number of iterations so that the
+  // warp-uniform shortcut can use full-warp votes.
+  const size_t warp_first = gtid - lane;
+  for (size_t base = warp_first; base < n; base += stride) {
+    const size_t i = base + lane;
+    const bool valid = i < n;
+    U k = valid ? radix_key_rt<U>(keys[i], kind, desc) : U(0);
+    const bool full = __all_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int p = 0; p < PASSES; ++p) {
+      const uint32_t d = uint32_t(k >> (p * kRadixBits)) & (kRadix - 1);
+      const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+      if (full && __all_sync(0xffffffffu, d == d0)) {
+        if (lane == 0) atomicAdd(&sh[p][d0], 32u);
+      } else if (valid) {
+        atomicAdd(&sh[p][d], 1u);
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) {
+    const uint32_t c = (&sh[0][0])[i];
+    if (c) atomicAdd(&hist[i], c);
+  }
+}
+
+// 2. Digit start offsets per pass, pass skipping and buffer schedule.
+__global__ void __launch_bounds__(kRadix)
+radix_prep_kernel(uint32_t *__restrict__ hist, int passes, uint32_t n,
+                  SortControl *__restrict__ ctrl) {
+  __shared__ uint32_t warp_sum[kRadix / kWarp];
+  __shared__ uint32_t skip[8];
+  const unsigned d = threadIdx.x, lane = lane_id(), w = d / kWarp;
+  for (int p = 0; p < passes; ++p) {
+    const uint32_t c = hist[p * kRadix + d];
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < kWarp; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (int(lane) >= o) incl += t;
+    }
+    if (lane == kWarp - 1) warp_sum[w] = incl;
+    __syncthreads();
+    uint32_t before = 0;
+    for (unsigned j = 0; j < w; ++j) before += warp_sum[j];
+    const int all_one = __syncthreads_or(c == n);
+    hist[p * kRadix + d] = before + incl - c;  // exclusive start of digit d
+    if (d == 0) skip[p] = all_one ? 1u : 0u;
+    __syncthreads();
+  }
+  if (d == 0) {
+    uint32_t alt = 0;
+    for (int p = 0; p < 8; ++p) {
+      const uint32_t sk = p < passes ? skip[p] : 1u;
+      ctrl->skip[p] = sk;
+      ctrl->src_alt[p] = alt;
+      if (!sk) alt ^= 1u;
+    }
+    ctrl->final_alt = alt;
+  }
+}
+
+// 3. One onesweep pass over digit `pass`.
+template <class U, int VB>
+__global__ void __launch_bounds__(kSortThreads)
+radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
+                      typename value_type_of<VB>::type *__restrict__ vals_main,
+                      typename value_type_of<VB>::type *__restrict__ vals_alt, uint32_t n,
+                      int pass, int kind, int desc, const uint32_t *__restrict__ digit_start,
+                      uint32_t *__restrict__ status, uint32_t *__restrict__ tile_counter,
+                      const SortControl *__restrict__ ctrl, uint32_t *err) {
+  typedef typename value_type_of<VB>::type VT;
+  constexpr int IPT = items_per_thread<U>::value;
+  constexpr int TILE = kSortThreads * IPT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // Shared layout: [warp digit counters][keys staging][values staging]
+  uint32_t *wcnt = reinterpret_cast<uint32_t *>(smem_raw);  // [kSortWarps][kRadix]
+  U *s_keys = reinterpret_cast<U *>(smem_raw + kSortWarps * kRadix * 4);
+  VT *s_vals = reinterpret_cast<VT *>(smem_raw + kSortWarps * kRadix * 4 + TILE * sizeof(U));
+  __shared__ uint32_t s_local_start[kRadix];
+  __shared__ uint32_t s_adj[kRadix];  // global base - local start, per digit
+  __shared__ uint32_t s_warp_sum[kRadix / kWarp];
+  __shared__ uint32_t s_tile;
+
+  if (ctrl->skip[pass]) return;
+  const bool from_alt = ctrl->src_alt[pass] != 0;
+  const U *__restrict__ src_k = from_alt ? keys_alt : keys_main;
+  U *__restrict__ dst_k = from_alt ? keys_main : keys_alt;
+  const VT *__restrict__ src_v = from_alt ? vals_alt : vals_main;
+  VT *__restrict__ dst_v = from_alt ? vals_main : vals_alt;
+
+  const unsigned tid = threadIdx.x, lane = lane_id(), warp = tid / kWarp;
+  const int shift = pass * kRadixBits;
+  for (int i = lane; i < kRadix; i += kWarp) wcnt[warp * kRadix + i] = 0;
+  if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t tile_base = tile * uint32_t(TILE);
+  const uint32_t warp_base = tile_base + warp * (kWarp * IPT);
+
+  // Load keys (and values) warp-striped: item i of lane l is element
+  // warp_base + i*32 + l, so ranking items in (i, l) order is input order.
+  U key[IPT];
+  VT val[VB ? IPT : 1];
+#pragma unroll
+  for (int i = 0; i < IPT; ++i) {
+    const uint32_t idx = warp_base + i * kWarp + lane;
+    key[i] = idx < n ? src_k[idx] : U(0);
+  }
+  if (VB) {
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const uint32_t idx = warp_base + i * kWarp + lane;
+      if (idx < n) val[i] = src_v[idx];
+    }
+  }
+
+  // Rank: per item, lanes with equal digits form a match group; the group's
+  // lowest lane advances the warp's counter for that digit.
+  uint32_t dr[IPT];  // digit | rank-within-warp << 8 | invalid << 31
+  const unsigned lt = lanemask_lt();
+#pragma unroll
+  for (int i = 0; i < IPT; ++i) {
+    const uint32_t idx = warp_base + i * kWarp + lane;
+    const bool valid = idx < n;
+    const uint32_t d = valid ? (uint32_t(radix_key_rt<U>(key[i], kind, desc) >> shift) & (kRadix - 1)) : 0x100u;
+    const unsigned grp = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(grp) - 1;
+    uint32_t old = 0;
+    if (valid && int(lane) == leader) {
+      old = wcnt[warp * kRadix + d];
+      wcnt[warp * kRadix + d] = old + __popc(grp);
+    }
+    old = __shfl_sync(0xffffffffu, old, leader);
+    dr[i] = valid ? (d | ((old + __popc(grp & lt)) << 8)) : 0x80000000u;
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // Per digit (thread d): exclusive prefix across warps, tile count, publish.
+  uint32_t tile_cnt = 0;
+  if (tid < kRadix) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+      const uint32_t c = wcnt[w * kRadix + tid];
+      wcnt[w * kRadix + tid] = run;
+      run += c;
+    }
+    tile_cnt = run;
+    uint32_t *st = status + size_t(tile) * kRadix + tid;
+    if (tile == 0) st_release_u32(st, kStPrefix | tile_cnt);
+    else st_release_u32(st, kStAggregate | tile_cnt);
+  }
+  // Tile-local exclusive scan of the digit counts (threads 0..255).
+  uint32_t incl = tile_cnt;
+#pragma unroll
+  for (int o = 1; o < kWarp; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (int(lane) >= o) incl += t;
+  }
+  if (tid < kRadix && lane == kWarp - 1) s_warp_sum[warp] = incl;
+  __syncthreads();
+  if (tid < kRadix) {
+    uint32_t before = 0;
+    for (unsigned j = 0; j < warp; ++j) before += s_warp_sum[j];
+    const uint32_t local_start = before + incl - tile_cnt;
+    s_local_start[tid] = local_start;
+    // Decoupled look-back for digit tid.
+    uint32_t excl = 0;
+    if (tile > 0) {
+      int64_t t = int64_t(tile) - 1;
+      bool gave_up = false;
+      while (t >= 0) {
+        const uint32_t *p = status + size_t(t) * kRadix + tid;
+        uint32_t w = ld_acquire_u32(p);
+        uint32_t spins = 0;
+        while ((w >> kStFlagShift) == 0) {
+          if (++spins > kSpinLimit) {
+            gave_up = true;
+            break;
+          }
+          __nanosleep(spins < 32 ? 20 : 200);
+          w = ld_acquire_u32(p);
+        }
+        if (gave_up) break;
+        excl += w & kStValueMask;
+        if ((w & kStPrefix) == kStPrefix && (w >> kStFlagShift) == 2u) break;
+        --t;
+      }
+      if (gave_up) report_error(err, kErrLookbackTimeout);
+      st_release_u32(status + size_t(tile) * kRadix + tid, kStPrefix | ((excl + tile_cnt) & kStValueMask));
+    }
+    s_adj[tid] = digit_start[pass * kRadix + tid] + excl - local_start;
+  }
+  __syncthreads();
+
+  // Stage keys and values in digit order.
+#pragma unroll
+  for (int i = 0; i < IPT; ++i) {
+    if (!(dr[i] & 0x80000000u)) {
+      const uint32_t d = dr[i] & 0xffu;
+      const uint32_t pos = s_local_start[d] + wcnt[warp * kRadix + d] + (dr[i] >> 8);
+      s_keys[pos] = key[i];
+      if (VB) s_vals[pos] = val[i];
+    }
+  }
+  __syncthreads();
+
+  // Write out: consecutive threads take consecutive staged elements, so each
+  // digit's run is written to consecutive addresses.
+  const uint32_t tile_valid = (n - tile_base) < uint32_t(TILE) ? (n - tile_base) : uint32_t(TILE);
+#pragma unroll
+  for (int k = 0; k < IPT; ++k) {
+    const uint32_t idx = k * kSortThreads + tid;
+    if (idx < tile_valid) {
+      const U kv = s_keys[idx];
+      const uint32_t d = uint32_t(radix_key_rt<U>(kv, kind, desc) >> shift) & (kRadix - 1);
+      const uint32_t dst = s_adj[d] + idx;
+      dst_k[dst] = kv;
+      if (VB) dst_v[dst] = s_vals[idx];
+    }
+  }
+}
+
+// 4. Copy the result back when it ended in the temporary buffers.
+template <class U, int VB>
+__global__ void radix_copyback_kernel(U *__restrict__ keys_main, const U *__restrict__ keys_alt,
+                                      typename value_type_of<VB>::type *__restrict__ vals_main,
+                                      const typename value_type_of<VB>::type *__restrict__ vals_alt,
+                                      size_t n, const SortControl *__restrict__ ctrl) {
+  if (!ctrl->final_alt) return;
+  const size_t stride = size_t(gridDim.x) * blockDim.x;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    keys_main[i] = keys_alt[i];
+    if (VB) vals_main[i] = vals_alt[i];
+  }
+}
+
+// Serial insertion sort by one thread with the functor's comparison on the
+// typed keys (insertion_sort.hpp:26-159): value moves left while
+// compare(value, previous) holds.
+template <class T, int VB>
+__global__ void insertion_sort_kernel(T *__restrict__ keys, typename value_type_of<VB>::type *__restrict__ vals,
+                                      int n, int desc) {
+  typedef typename value_type_of<VB>::type VT;
+  T k[32];
+  VT v[VB ? 32 : 1];
+  for (int i = 0; i < n; ++i) {
+    k[i] = keys[i];
+    if (VB) v[i] = vals[i];
+  }
+  for (int i = 1; i < n; ++i) {
+    const T key = k[i];
+    VT value;
+    if (VB) value = v[i];
+    int pos = i;
+    while (pos > 0 && (desc ? (key > k[pos - 1]) : (key < k[pos - 1]))) {
+      k[pos] = k[pos - 1];
+      if (VB) v[pos] = v[pos - 1];
+      --pos;
+    }
+    k[pos] = key;
+    if (VB) v[pos] = value;
+  }
+  for (int i = 0; i < n; ++i) {
+    keys[i] = k[i];
+    if (VB) vals[i] = v[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct SortLayout {
+  size_t alt_keys = 0, alt_vals = 0, hist = 0, ctrl = 0, counters = 0, status = 0, total = 0;
+  size_t zero_begin = 0, zero_bytes = 0;
+  uint32_t tiles = 0;
+};
+
+template <class U>
+SortLayout sort_layout(size_t n, size_t vb, int passes) {
+  constexpr int IPT = items_per_thread<U>::value;
+  SortLayout L;
+  L.tiles = uint32_t(div_up(n, size_t(kSortThreads) * IPT));
+  size_t off = 0;
+  L.alt_keys = off;
+  off += align256(n * sizeof(U));
+  L.alt_vals = off;
+  off += align256(n * vb);
+  L.hist = off;
+  off += align256(size_t(passes) * kRadix * 4);
+  L.ctrl = off;
+  off += 256;
+  L.counters = off;
+  off += 256;
+  L.status = off;
+  off += align256(size_t(passes) * L.tiles * kRadix * 4);
+  L.total = off;
+  L.zero_begin = L.hist;
+  L.zero_bytes = off - L.hist;
+  return L;
+}
+
+template <class U, int VB>
+bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int kind, int desc,
+                        void *temp, size_t *temp_bytes) {
+  typedef typename value_type_of<VB>::type VT;
+  constexpr int PASSES = int(sizeof(U));
+  constexpr int IPT = items_per_thread<U>::value;
+  constexpr int TILE = kSortThreads * IPT;
+  BCX_CHECK(n < kMaxSortN, BCX_INVALID_VALUE, "radix sort: n must be below 2^30 (got %zu)", n);
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
+  const SortLayout L = sort_layout<U>(n, VB, PASSES);
+  if (n < 2 && !(temp == nullptr && temp_bytes != nullptr)) return BCX_SUCCESS;
+  TempStorage ts;
+  bool query = false;
+  rc = ts.acquire(temp, temp_bytes, L.total, s, &query);
+  if (rc || query) return rc;
+  char *base = static_cast<char *>(ts.ptr());
+  U *k_main = static_cast<U *>(keys);
+  U *k_alt = reinterpret_cast<U *>(base + L.alt_keys);
+  VT *v_main = static_cast<VT *>(values);
+  VT *v_alt = VB ? reinterpret_cast<VT *>(base + L.alt_vals) : nullptr;
+  uint32_t *hist = reinterpret_cast<uint32_t *>(base + L.hist);
+  SortControl *ctrl = reinterpret_cast<SortControl *>(base + L.ctrl);
+  uint32_t *counters = reinterpret_cast<uint32_t *>(base + L.counters);
+  uint32_t *status = reinterpret_cast<uint32_t *>(base + L.status);
+  BCX_CUDA(cudaMemsetAsync(base + L.zero_begin, 0, L.zero_bytes, s));
+  {
+    KernelScope ks("radix_histogram", s);
+    size_t blocks = div_up(n, size_t(kHistThreads) * 16);
+    size_t cap = size_t(ds->sm_count) * 4;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    radix_histogram_kernel<U, PASSES><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, kind, desc, hist);
+    rc = launch_status("radix_histogram");
+    if (rc) return rc;
+  }
+  {
+    KernelScope ks("radix_prep", s);
+    radix_prep_kernel<<<1, kRadix, 0, s>>>(hist, PASSES, uint32_t(n), ctrl);
+    rc = launch_status("radix_prep");
+    if (rc) return rc;
+  }
+  const size_t smem = size_t(kSortWarps) * kRadix * 4 + size_t(TILE) * sizeof(U) + (VB ? size_t(TILE) * sizeof(VT) : 0);
+  static bool attr_set = false;
+  if (!attr_set) {
+    BCX_CUDA(cudaFuncSetAttribute(radix_onesweep_kernel<U, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    attr_set = true;
+  }
+  for (int p = 0; p < PASSES; ++p) {
+    KernelScope ks("radix_onesweep", s);
+    radix_onesweep_kernel<U, VB><<<L.tiles, kSortThreads, smem, s>>>(
+        k_main, k_alt, v_main, v_alt, uint32_t(n), p, kind, desc, hist, status + size_t(p) * L.tiles * kRadix,
+        counters + p, ctrl, ds->err_word);
+    rc = launch_status("radix_onesweep");
+    if (rc) return rc;
+  }
+  KernelScope ks("radix_copyback", s);
+  size_t blocks = div_up(n, 256);
+  size_t cap = size_t(ds->sm_count) * 8;
+  if (blocks > cap) blocks = cap;
+  radix_copyback_kernel<U, VB><<<unsigned(blocks), 256, 0, s>>>(k_main, k_alt, v_main, v_alt, n, ctrl);
+  return launch_status("radix_copyback");
+}
+
+template <class T, int VB>
+bcx_status insertion_t(cudaStream_t s, void *keys, void *values, size_t n, int desc) {
+  typedef typename value_type_of<VB>::type VT;
+  KernelScope ks("insertion_sort", s);
+  insertion_sort_kernel<T, VB><<<1, 1, 0, s>>>(static_cast<T *>(keys), static_cast<VT *>(values), int(n), desc);
+  return launch_status("insertion_sort");
+}
+
+int key_kind(bcx_dtype t) {
+  if (t == BCX_FLOAT || t == BCX_DOUBLE) return kKeyFloat;
+  if (t == BCX_CHAR || t == BCX_SHORT || t == BCX_INT || t == BCX_LONG) return kKeySigned;
+  return kKeyUnsigned;
+}
+
+template <class U>
+bcx_status radix_by_vb(cudaStream_t s, size_t vb, void *k, void *v, size_t n, int kind, int desc,
+                       void *temp, size_t *tb) {
+  switch (vb) {
+    case 0: return radix_sort_t<U, 0>(s, k, v, n, kind, desc, temp, tb);
+    case 1: return radix_sort_t<U, 1>(s, k, v, n, kind, desc, temp, tb);
+    case 2: return radix_sort_t<U, 2>(s, k, v, n, kind, desc, temp, tb);
+    case 4: return radix_sort_t<U, 4>(s, k, v, n, kind, desc, temp, tb);
+    case 8: return radix_sort_t<U, 8>(s, k, v, n, kind, desc, temp, tb);
+    case 16: return radix_sort_t<U, 16>(s, k, v, n, kind, desc, temp, tb);
+  }
+  set_error("radix sort: value size %zu not in {1,2,4,8,16}", vb);
+  return BCX_INVALID_VALUE;
+}
+
+bcx_status radix_entry(cudaStream_t s, bcx_dtype kt, size_t vb, void *keys, void *values, size_t n,
+                       int desc, void *temp, size_t *tb) {
+  BCX_CHECK(dtype_valid(kt), BCX_INVALID_VALUE, "invalid key dtype %d", int(kt));
+  BCX_CHECK(n == 0 || keys != nullptr, BCX_INVALID_VALUE, "keys is NULL");
+  BCX_CHECK(vb == 0 || n == 0 || values != nullptr, BCX_INVALID_VALUE, "values is NULL");
+  const int kind = key_kind(kt);
+  desc = desc ? 1 : 0;
+  switch (dtype_size(kt)) {
+    case 1: return radix_by_vb<uint8_t>(s, vb, keys, values, n, kind, desc, temp, tb);
+    case 2: return radix_by_vb<uint16_t>(s, vb, keys, values, n, kind, desc, temp, tb);
+    case 4: return radix_by_vb<uint32_t>(s, vb, keys, values, n, kind, desc, temp, tb);
+    case 8: return radix_by_vb<unsigned long long>(s, vb, keys, values, n, kind, desc, temp, tb);
+  }
+  return BCX_INVALID_VALUE;
+}
+
+template <class T>
+bcx_status insertion_by_vb(cudaStream_t s, size_t vb, void *k, void *v, size_t n, int desc) {
+  switch (vb) {
+    case 0: return insertion_t<T, 0>(s, k, v, n, desc);
+    case 1: return insertion_t<T, 1>(s, k, v, n, desc);
+    case 2: return insertion_t<T, 2>(s, k, v, n, desc);
+    case 4: return insertion_t<T, 4>(s, k, v, n, desc);
+    case 8: return insertion_t<T, 8>(s, k, v, n, desc);
+    case 16: return insertion_t<T, 16>(s, k, v, n, desc);
+  }
+  set_error("sort: value size %zu not in {1,2,4,8,16}", vb);
+  return BCX_INVALID_VALUE;
+}
+
+bcx_status insertion_entry(cudaStream_t s, bcx_dtype kt, size_t vb, void *k, void *v, size_t n, int desc) {
+  switch (kt) {
+    case BCX_CHAR: return insertion_by_vb<int8_t>(s, vb, k, v, n, desc);
+    case BCX_UCHAR: return insertion_by_vb<uint8_t>(s, vb, k, v, n, desc);
+    case BCX_SHORT: return insertion_by_vb<int16_t>(s, vb, k, v, n, desc);
+    case BCX_USHORT: return insertion_by_vb<uint16_t>(s, vb, k, v, n, desc);
+    case BCX_INT: return insertion_by_vb<int32_t>(s, vb, k, v, n, desc);
+    case BCX_UINT: return insertion_by_vb<uint32_t>(s, vb, k, v, n, desc);
+    case BCX_LONG: return insertion_by_vb<long long>(s, vb, k, v, n, desc);
+    case BCX_ULONG: return insertion_by_vb<unsigned long long>(s, vb, k, v, n, desc);
+    case BCX_FLOAT: return insertion_by_vb<float>(s, vb, k, v, n, desc);
+    case BCX_DOUBLE: return insertion_by_vb<double>(s, vb, k, v, n, desc);
+  }
+  return BCX_INVALID_VALUE;
+}
+
+}  // namespace
+}  // namespace bcx
+
+using namespace bcx;
+
+extern "C" {
+
+bcx_status bcx_radix_sort_keys(bcx_stream stream, bcx_dtype key_type, void *keys, size_t n,
+                               int descending, void *temp, size_t *temp_bytes) {
+  clear_error();
+  return radix_entry((cudaStream_t)stream, key_type, 0, keys, nullptr, n, descending, temp, temp_bytes);
+}
+
+bcx_status bcx_radix_sort_pairs(bcx_stream stream, bcx_dtype key_type, size_t value_bytes, void *keys,
+                                void *values, size_t n, int descending, void *temp,
+                                size_t *temp_bytes) {
+  clear_error();
+  BCX_CHECK(value_bytes != 0, BCX_INVALID_VALUE, "value_bytes is 0");
+  return radix_entry((cudaStream_t)stream, key_type, value_bytes, keys, values, n, descending, temp,
+                     temp_bytes);
+}
+
+bcx_status bcx_sort_keys(bcx_stream stream, bcx_dtype key_type, void *keys, size_t n, int descending,
+                         void *temp, size_t *temp_bytes) {
+  clear_error();
+  BCX_CHECK(dtype_valid(key_type), BCX_INVALID_VALUE, "invalid key dtype %d", int(key_type));
+  if (n <= 32) {
+    if (temp == nullptr && temp_bytes != nullptr) {
+      *temp_bytes = 0;
+      return BCX_SUCCESS;
+    }
+    if (n < 2) return BCX_SUCCESS;
+    return insertion_entry((cudaStream_t)stream, key_type, 0, keys, nullptr, n, descending ? 1 : 0);
+  }
+  return radix_entry((cudaStream_t)stream, key_type, 0, keys, nullptr, n, descending, temp, temp_bytes);
+}
+
+bcx_status bcx_sort_pairs(bcx_stream stream, bcx_dtype key_type, size_t value_bytes, void *keys,
+                          void *values, size_t n, int descending, void *temp, size_t *temp_bytes) {
+  clear_error();
+  BCX_CHECK(dtype_valid(key_type), BCX_INVALID_VALUE, "invalid key dtype %d", int(key_type));
+  BCX_CHECK(value_bytes != 0, BCX_INVALID_VALUE, "value_bytes is 0");
+  if (n < 32) {
+    if (temp == nullptr && temp_bytes != nullptr) {
+      *temp_bytes = 0;
+      return BCX_SUCCESS;
+    }
+    if (n < 2) return BCX_SUCCESS;
+    return insertion_entry((cudaStream_t)stream, key_type, value_bytes, keys, values, n, descending ? 1 : 0);
+  }
+  return radix_entry((cudaStream_t)stream, key_type, value_bytes, keys, values, n, descending, temp,
+                     temp_bytes);
+}
+
+bcx_status bcx_sort_pairs_host(bcx_stream stream, bcx_dtype key_type, size_t value_bytes,
+                               void *host_keys, void *host_values, size_t n, int descending) {
+  clear_error();
+  BCX_CHECK(dtype_valid(key_type), BCX_INVALID_VALUE, "invalid key dtype %d", int(key_type));
+  if (n == 0) return BCX_SUCCESS;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t kb = n * dtype_size(key_type), vb = n * value_bytes;
+  void *dk = nullptr, *dv = nullptr;
+  BCX_CUDA(cudaMallocAsync(&dk, kb, s));
+  if (vb) {
+    cudaError_t e = cudaMallocAsync(&dv, vb, s);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(dk, s);
+      return cuda_status(e, "cudaMallocAsync(values)");
+    }
+  }
+  bcx_status rc = BCX_SUCCESS;
+  cudaError_t e = cudaMemcpyAsync(dk, host_keys, kb, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && vb) e = cudaMemcpyAsync(dv, host_values, vb, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) rc = cuda_status(e, "copy to device");
+  if (!rc) {
+    rc = vb ? bcx_sort_pairs(stream, key_type, value_bytes, dk, dv, n, descending, nullptr, nullptr)
+            : bcx_sort_keys(stream, key_type, dk, n, descending, nullptr, nullptr);
+  }
+  if (!rc) {
+    e = cudaMemcpyAsync(host_keys, dk, kb, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && vb) e = cudaMemcpyAsync(host_values, dv, vb, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) rc = cuda_status(e, "copy to host");
+  }
+  cudaFreeAsync(dk, s);
+  if (dv) cudaFreeAsync(dv, s);
+  e = cudaStreamSynchronize(s);
+  if (!rc && e != cudaSuccess) rc = cuda_status(e, "cudaStreamSynchronize");
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,199 @@
+/*
+ * bcx.h -- C ABI of libbcx, the GB300 (sm_103a) data-parallel core behind the
+ * boost::compute algorithm headers.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and returns
+ * a bcx_status.  Status values equal the OpenCL cl_int error codes wherever an
+ * OpenCL counterpart exists, so a header can rethrow them unchanged as
+ * boost::compute::opencl_error(status).
+ *
+ * Calling convention (mirrors the reference's queue-ordered algorithms,
+ * include/boost/compute/command_queue.hpp:1403-1495):
+ *   - all compute calls are asynchronous on the given stream (a cudaStream_t;
+ *     NULL = the legacy default stream) and return once work is enqueued;
+ *   - device pointers are raw CUDA device (or managed) pointers;
+ *   - temporary storage follows a query/run pair: pass temp == NULL with a
+ *     non-NULL temp_bytes to receive the size needed, then call again with
+ *     temp pointing at that many bytes of device memory.  Passing
+ *     temp == NULL and temp_bytes == NULL lets the library take the temporary
+ *     from a stream-ordered pool (cudaMallocAsync) and release it on the
+ *     stream after the work (the reference allocates temporaries per call,
+ *     algorithm/detail/radix_sort.hpp:333-336);
+ *   - no C++ exception crosses this ABI; bcx_last_error_string() describes the
+ *     last failure on the calling thread.
+ */
+#ifndef BCX_H
+#define BCX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int bcx_status;
+typedef void *bcx_stream; /* a cudaStream_t */
+
+/* ---- status codes ------------------------------------------------------ */
+#define BCX_SUCCESS                   0
+#define BCX_DEVICE_NOT_FOUND         -1   /* CL_DEVICE_NOT_FOUND */
+#define BCX_MEM_ALLOCATION_FAILURE   -4   /* CL_MEM_OBJECT_ALLOCATION_FAILURE */
+#define BCX_OUT_OF_RESOURCES         -5   /* CL_OUT_OF_RESOURCES (CUDA runtime error) */
+#define BCX_BUILD_PROGRAM_FAILURE   -11   /* CL_BUILD_PROGRAM_FAILURE (NVRTC) */
+#define BCX_INVALID_VALUE           -30   /* CL_INVALID_VALUE */
+#define BCX_INVALID_KERNEL_NAME     -46   /* CL_INVALID_KERNEL_NAME */
+#define BCX_INVALID_BUFFER_SIZE     -61   /* CL_INVALID_BUFFER_SIZE */
+#define BCX_DEVICE_TIMEOUT        -9001   /* a bounded device-side wait gave up */
+#define BCX_UNSUPPORTED           -9002   /* dtype/op combination not provided */
+
+/* ---- element types (the radix-sortable fundamentals of
+ *      algorithm/detail/radix_sort.hpp:41-47) ------------------------------ */
+typedef enum {
+    BCX_CHAR = 0, BCX_UCHAR = 1, BCX_SHORT = 2, BCX_USHORT = 3,
+    BCX_INT = 4, BCX_UINT = 5, BCX_LONG = 6, BCX_ULONG = 7,
+    BCX_FLOAT = 8, BCX_DOUBLE = 9
+} bcx_dtype;
+
+/* ---- built-in binary functors (functional/operator.hpp:57-92,
+ *      functional/integer.hpp:24-25) -------------------------------------- */
+typedef enum {
+    BCX_PLUS = 0, BCX_MULTIPLIES = 1, BCX_MIN = 2, BCX_MAX = 3,
+    BCX_BIT_AND = 4, BCX_BIT_OR = 5, BCX_BIT_XOR = 6,
+    BCX_MINUS = 7, BCX_DIVIDES = 8, BCX_MODULUS = 9
+} bcx_op;
+
+/* ---- built-in unary functors used by transform (functional/math.hpp,
+ *      functional/operator.hpp) ------------------------------------------- */
+typedef enum {
+    BCX_IDENTITY = 0, BCX_NEGATE = 1, BCX_ABS = 2, BCX_SQRT = 3,
+    BCX_LOGICAL_NOT = 4, BCX_BIT_NOT = 5
+} bcx_unary_op;
+
+/* ---- runtime (replaces system.hpp / device.hpp / command_queue.hpp /
+ *      buffer.hpp for the hot path) --------------------------------------- */
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+bcx_status bcx_get_version(int *version);
+/* Text of the last failure on the calling thread ("" if none). */
+const char *bcx_last_error_string(void);
+/* system::devices() count -- system.hpp:181 */
+bcx_status bcx_device_count(int *count);
+/* Make `device` current for this thread (context selection, system.hpp:235-298). */
+bcx_status bcx_set_device(int device);
+/* device::name(), compute_units(), global_memory_size() -- device.hpp */
+bcx_status bcx_device_info(int device, char *name, size_t name_len,
+                           int *compute_units, size_t *global_mem_bytes);
+/* command_queue(context, device) -- command_queue.hpp:78 */
+bcx_status bcx_stream_create(bcx_stream *stream);
+bcx_status bcx_stream_destroy(bcx_stream stream);
+/* command_queue::finish() -- command_queue.hpp:1564 */
+bcx_status bcx_stream_synchronize(bcx_stream stream);
+/* buffer(context, size) -- buffer.hpp; freed by bcx_free */
+bcx_status bcx_malloc(void **ptr, size_t bytes);
+bcx_status bcx_free(void *ptr);
+/* Page-locked host memory (allocator/pinned_allocator.hpp). */
+bcx_status bcx_malloc_host(void **ptr, size_t bytes);
+bcx_status bcx_free_host(void *ptr);
+/* enqueue_copy_buffer / enqueue_read_buffer / enqueue_write_buffer
+ * (command_queue.hpp:400-700), direction inferred from the pointers. */
+bcx_status bcx_memcpy_async(void *dst, const void *src, size_t bytes, bcx_stream stream);
+/* enqueue_fill_buffer with a byte pattern (command_queue.hpp:1250). */
+bcx_status bcx_memset_async(void *dst, int byte_value, size_t bytes, bcx_stream stream);
+/* Synchronizes `stream`, then reports and clears any bounded device-side wait
+ * that expired in this library's kernels since the last check
+ * (BCX_DEVICE_TIMEOUT), or BCX_SUCCESS. */
+bcx_status bcx_device_error_check(bcx_stream stream);
+
+/* ---- sort ---------------------------------------------------------------
+ * Radix path of detail::radix_sort / radix_sort_by_key
+ * (algorithm/detail/radix_sort.hpp:253-462).  Keys are ordered by the
+ * reference's radix() key transform (radix_sort.hpp:100-127) and the sort is
+ * stable, so equal keys keep their input order and values follow their keys.
+ * In place on `keys` (and `values`); any n. value_bytes in {1,2,4,8,16}. */
+bcx_status bcx_radix_sort_keys(bcx_stream stream, bcx_dtype key_type, void *keys,
+                               size_t n, int descending,
+                               void *temp, size_t *temp_bytes);
+bcx_status bcx_radix_sort_pairs(bcx_stream stream, bcx_dtype key_type,
+                                size_t value_bytes, void *keys, void *values,
+                                size_t n, int descending,
+                                void *temp, size_t *temp_bytes);
+/* Public compute::sort / sort_by_key dispatch for less<T> (descending = 0) and
+ * greater<T> (descending = 1): sort.hpp:34-80 (n < 2 nothing, n <= 32 serial
+ * insertion sort with the comparator, else radix) and sort_by_key.hpp:33-83
+ * (n < 32 serial insertion sort by key, else radix). */
+bcx_status bcx_sort_keys(bcx_stream stream, bcx_dtype key_type, void *keys,
+                         size_t n, int descending,
+                         void *temp, size_t *temp_bytes);
+bcx_status bcx_sort_pairs(bcx_stream stream, bcx_dtype key_type,
+                          size_t value_bytes, void *keys, void *values,
+                          size_t n, int descending,
+                          void *temp, size_t *temp_bytes);
+/* compute::sort_by_key on host iterators: copies keys/values from host
+ * memory, sorts them on the device, copies them back and synchronizes
+ * (the host-iterator sort path, sort.hpp:125-148). */
+bcx_status bcx_sort_pairs_host(bcx_stream stream, bcx_dtype key_type,
+                               size_t value_bytes, void *host_keys,
+                               void *host_values, size_t n, int descending);
+
+/* ---- scan ---------------------------------------------------------------
+ * exclusive_scan / inclusive_scan (exclusive_scan.hpp:55-104,
+ * inclusive_scan.hpp:53-87, detail/scan_on_gpu.hpp:187-324).
+ * out[i] = init op in[0] op ... op in[i-1] (exclusive; out[0] = init) or
+ * in[0] op ... op in[i] (inclusive; init ignored).  `init` points at one
+ * host value of `type` (NULL = 0).  in == out is allowed.  compensated = 1
+ * with BCX_FLOAT/BCX_DOUBLE plus selects Neumaier-compensated tile sums with
+ * an FP64 carry between tiles. */
+bcx_status bcx_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive,
+                    const void *init, const void *in, void *out, size_t n,
+                    int compensated, void *temp, size_t *temp_bytes);
+
+/* ---- reduce / accumulate -------------------------------------------------
+ * reduce(first, last, result, op) into ONE device value at out_dev
+ * (reduce.hpp:205-305, detail/reduce_on_gpu.hpp:169-280).  n == 0 writes
+ * nothing (reduce.hpp:291-296).  Integer results are exact (mod 2^bits);
+ * compensated = 1 with float plus uses Neumaier sums in warps and blocks and
+ * an FP64 combine of the block partials. */
+bcx_status bcx_reduce(bcx_stream stream, bcx_dtype type, bcx_op op,
+                      const void *in, size_t n, void *out_dev, int compensated,
+                      void *temp, size_t *temp_bytes);
+/* accumulate(first, last, init, op) (accumulate.hpp:102-188): the value
+ * init op reduce(in) written to out_dev; `init` is one host value; n == 0
+ * writes init. */
+bcx_status bcx_accumulate(bcx_stream stream, bcx_dtype type, bcx_op op,
+                          const void *in, size_t n, const void *init,
+                          void *out_dev, int compensated,
+                          void *temp, size_t *temp_bytes);
+
+/* ---- transform -----------------------------------------------------------
+ * transform(first, last, result, f) = copy(transform_iterator) on the device
+ * (transform.hpp:38-82, detail/copy_on_device.hpp:60-92). */
+bcx_status bcx_transform_unary(bcx_stream stream, bcx_dtype type, bcx_unary_op op,
+                               const void *in, void *out, size_t n);
+/* transform(first1, last1, first2, result, op) with a built-in functor. */
+bcx_status bcx_transform_binary(bcx_stream stream, bcx_dtype type, bcx_op op,
+                                const void *in0, const void *in1, void *out,
+                                size_t n);
+/* transform(x, x+n, y, r, alpha*_1 + _2) (perf/perf_saxpy.cpp:50-56) for
+ * float/double: r[i] = fma(alpha, x[i], y[i]) (single rounding). `alpha`
+ * points at one host value of `type`. */
+bcx_status bcx_transform_saxpy(bcx_stream stream, bcx_dtype type, const void *alpha,
+                               const void *x, const void *y, void *out, size_t n);
+
+/* ---- profiling (command_queue::enable_profiling / event::duration,
+ *      command_queue.hpp:82, event.hpp:269) --------------------------------
+ * When enabled, every kernel this library launches is bracketed by CUDA
+ * events on its stream; bcx_profile_read sums the durations per kernel name
+ * (synchronizing first).  Names are "<family>" strings such as
+ * "radix_onesweep", "scan_lookback", "reduce_partials". */
+bcx_status bcx_profile_enable(int enable);
+bcx_status bcx_profile_reset(void);
+/* Fills up to `cap` entries; *count receives the number of kernel names. */
+bcx_status bcx_profile_read(char *names, size_t name_stride, uint64_t *launches,
+                            double *total_ms, size_t cap, size_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BCX_H */
