@@ -315,8 +315,12 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
       const U kv = s_keys[idx];
       const uint32_t d = uint32_t(radix_key_rt<U>(kv, kind, desc) >> shift) & (kRadix - 1);
       const uint32_t dst = s_adj[d] + idx;
-      dst_k[dst] = kv;
-      if (VB) dst_v[dst] = s_vals[idx];
+      // Always in range unless a look-back wait gave up (then the error word
+      // is set and the output is garbage, but no write leaves the buffer).
+      if (dst < n) {
+        dst_k[dst] = kv;
+        if (VB) dst_v[dst] = s_vals[idx];
+      }
     }
   }
 }
