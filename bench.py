@@ -207,6 +207,10 @@ def main():
     ap.add_argument("--impl", default="bcx", choices=["bcx", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "sort", "prims"],
+                    help="'sort' skips the other primitives, 'prims' skips the sort (profiling runs)")
+    ap.add_argument("--n-sort", type=int, default=N_SORT, help="pairs per sort (default 2^28)")
+    ap.add_argument("--n-scan", type=int, default=N_SCAN, help="scan/reduce elements (default 2^30)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -217,6 +221,11 @@ def main():
     import torch
 
     import compute_gb300 as bc
+    global N_SORT, N_SCAN
+    N_SORT = args.n_sort
+    N_SCAN = args.n_scan
+    if args.only == "prims":
+        N_SORT = 1 << 20
     rank, world, local = dist_init(args.gpus)
     torch.cuda.set_device(local)
     hbm, peak_kind = peaks()
@@ -275,6 +284,39 @@ def main():
     # ---- other primitives of the configuration ----------------------------
     prims = {}
     psteps = max(3, min(args.steps, 10))
+    if args.only == "sort":
+        psteps = 0
+    if psteps:
+        prims = run_primitives(torch, bc, dev, g, psteps, hbm)
+
+    # ---- e2e through the C ABI host-buffer entry point ---------------------
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(torch, bc, rank, world)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sort_baseline()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "uint32",
+                "data": "synthetic (seeded uniform 32-bit keys, iota values; BASELINE configs' shapes)",
+                "config": {"workload": WORKLOAD if N_SORT == 1 << 28 else f"sort_by_key uint32 pairs n={N_SORT}",
+                           "l2": "inputs larger than L2: every step sorts its own buffer",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "sorted_check": sorted_ok, "roofline": roofline, "kernel_share": kernel_share,
+                "gpu_launches": launches, "primitives": prims, "e2e": e2e, "cpu_baseline": cpu,
+                "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_primitives(torch, bc, dev, g, psteps, hbm):
+    prims = {}
     a = torch.randint(0, 100, (N_SCAN,), dtype=torch.int32, device=dev, generator=g)
     out = torch.empty_like(a)
     red = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -293,52 +335,32 @@ def main():
     prims["saxpy_f32_2p28"] = {"ms": ms, "GB/s": gbs, "frac": gbs / hbm, "bytes_per_elem": 12}
     del x, y, r
     torch.cuda.empty_cache()
+    return prims
 
-    # ---- e2e through the C ABI host-buffer entry point ---------------------
-    e2e = None
-    if not args.no_e2e:
-        import numpy as np
-        rng = np.random.default_rng(20261203 + rank)
-        hk0 = rng.integers(0, 2**32, size=N_SORT, dtype=np.uint64).astype(np.uint32)
-        hk = torch.from_numpy(hk0.view(np.int32)).pin_memory()
-        hv = torch.arange(N_SORT, dtype=torch.int32).pin_memory()
-        src_k = torch.from_numpy(hk0.view(np.int32))
-        src_v = torch.arange(N_SORT, dtype=torch.int32)
-        e2e_steps = 3
-        bc.sort_by_key_host(hk, hv, dtype="uint")  # warm-up
-        tot = 0.0
-        for _ in range(e2e_steps):
-            hk.copy_(src_k)
-            hv.copy_(src_v)
-            barrier(world)
-            t0 = time.perf_counter()
-            bc.sort_by_key_host(hk, hv, dtype="uint")
-            tot += time.perf_counter() - t0
-        tot = max_over_ranks(tot, world)
-        e2e = {"value": N_SORT * e2e_steps * world / tot / 1e9, "unit": "Gkeys/s",
-               "h2d_bytes_per_step": 8 * N_SORT, "d2h_bytes_per_step": 8 * N_SORT,
-               "ms_per_step": tot / e2e_steps * 1e3, "steps": e2e_steps,
-               "path": "bcx_sort_pairs_host (pinned host buffers)"}
-        del hk, hv, src_k, src_v
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        cpu = cpu_sort_baseline()
-
-    if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "uint32",
-                "data": "synthetic (seeded uniform 32-bit keys, iota values; BASELINE configs' shapes)",
-                "config": {"workload": WORKLOAD, "l2": "inputs larger than L2: every step sorts its own "
-                           "2 GiB buffer", "parallelism": "replicas" if world > 1 else "single GPU"},
-                "sorted_check": sorted_ok, "roofline": roofline, "kernel_share": kernel_share,
-                "gpu_launches": launches, "primitives": prims, "e2e": e2e, "cpu_baseline": cpu,
-                "clocks": clocks.summary()}
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+def run_e2e(torch, bc, rank, world):
+    import numpy as np
+    rng = np.random.default_rng(20261203 + rank)
+    hk0 = rng.integers(0, 2**32, size=N_SORT, dtype=np.uint64).astype(np.uint32)
+    hk = torch.from_numpy(hk0.view(np.int32)).pin_memory()
+    hv = torch.arange(N_SORT, dtype=torch.int32).pin_memory()
+    src_k = torch.from_numpy(hk0.view(np.int32))
+    src_v = torch.arange(N_SORT, dtype=torch.int32)
+    e2e_steps = 3
+    bc.sort_by_key_host(hk, hv, dtype="uint")  # warm-up
+    tot = 0.0
+    for _ in range(e2e_steps):
+        hk.copy_(src_k)
+        hv.copy_(src_v)
+        barrier(world)
+        t0 = time.perf_counter()
+        bc.sort_by_key_host(hk, hv, dtype="uint")
+        tot += time.perf_counter() - t0
+    tot = max_over_ranks(tot, world)
+    return {"value": N_SORT * e2e_steps * world / tot / 1e9, "unit": "Gkeys/s",
+            "h2d_bytes_per_step": 8 * N_SORT, "d2h_bytes_per_step": 8 * N_SORT,
+            "ms_per_step": tot / e2e_steps * 1e3, "steps": e2e_steps,
+            "path": "bcx_sort_pairs_host (pinned host buffers)"}
 
 
 if __name__ == "__main__":

@@ -64,6 +64,7 @@ SIGNATURES = {
     "bcx_transform_unary": (_i, [_vp, _i, _i, _vp, _vp, _sz]),
     "bcx_transform_binary": (_i, [_vp, _i, _i, _vp, _vp, _vp, _sz]),
     "bcx_transform_saxpy": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _sz]),
+    "bcx_reduce_by_key": (_i, [_vp, _i, _i, _i, _vp, _vp, _sz, _vp, _vp, _vp, _i, _vp, _szp]),
     "bcx_profile_enable": (_i, [_i]),
     "bcx_profile_reset": (_i, []),
     "bcx_profile_read": (_i, [C.c_char_p, _sz, C.POINTER(C.c_uint64), C.POINTER(C.c_double), _sz, _szp]),

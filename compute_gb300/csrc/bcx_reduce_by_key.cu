@@ -1,0 +1,367 @@
+// bcx_reduce_by_key.cu -- reduce_by_key in one pass over HBM.
+//
+// Reference: reduce_by_key (algorithm/reduce_by_key.hpp,
+// algorithm/detail/reduce_by_key.hpp:66-113) -> reduce_by_key_with_scan
+// (algorithm/detail/reduce_by_key_with_scan.hpp:432-486): a key-change flag
+// kernel plus an inclusive_scan to number the runs (:53-100), per-group
+// carry-outs (:105-180), carry-ins (:182-270) and a final Hillis-Steele
+// reduction by key (:272-400), then a blocking read of the run count.
+//
+// GB300 design: one kernel.  The operation is a segmented scan whose element
+// is (head?, run count, value) and whose combine (a then b) is
+//   (a.count + b.count, a.head | b.head, b.head ? b.value : a.value op b.value).
+// Each block takes the next tile from an atomic ticket, loads keys and values
+// warp-striped (coalesced), derives head flags from the previous key (warp
+// shuffles; one global load per warp), scans the triples with warp shuffles,
+// combines warps through shared memory and the tile with its predecessors by
+// decoupled look-back (order-preserving, bounded waits).  Run heads write the
+// output key, run ends write the reduced value, and the block holding the last
+// element writes the run count -- nothing is read back to the host.  Key
+// equality is the typed == of equal_to<T>.  Float plus with compensated=1
+// carries Neumaier (s, c) pairs.
+#include <cuda_runtime.h>
+
+#include "bcx.h"
+#include "bcx_common.cuh"
+#include "bcx_internal.h"
+
+namespace bcx {
+namespace {
+
+constexpr int kRbkThreads = 256;
+constexpr int kRbkWarps = kRbkThreads / kWarp;
+constexpr int kRbkItems = 8;
+constexpr int kRbkTile = kRbkThreads * kRbkItems;
+constexpr uint32_t kHeadBit = 0x80000000u;
+constexpr uint32_t kCountMask = 0x7fffffffu;
+enum : uint32_t { kRbInvalid = 0, kRbAggregate = 1, kRbPrefix = 2 };
+
+// Value policies.
+template <class V, template <class> class OpT>
+struct RbPlain {
+  typedef typename widen<V>::type Acc;
+  typedef OpT<Acc> Op;
+  __device__ __forceinline__ static Acc ident() { return Op::identity(); }
+  __device__ __forceinline__ static Acc from(V x) { return Acc(x); }
+  __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return Op()(a, b); }
+  __device__ __forceinline__ static V out(Acc a) { return V(a); }
+  __device__ __forceinline__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static Acc shfl_down(Acc a, int d) { return __shfl_down_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static Acc shfl(Acc a, int s) { return __shfl_sync(0xffffffffu, a, s); }
+};
+struct RbCompF32 {
+  typedef comp_f32 Acc;
+  __device__ __forceinline__ static Acc ident() { return comp_f32{0.f, 0.f}; }
+  __device__ __forceinline__ static Acc from(float x) { return comp_f32{x, 0.f}; }
+  __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return comp_merge(a, b); }
+  __device__ __forceinline__ static float out(Acc a) { return a.s + a.c; }
+  __device__ __forceinline__ static Acc shfl_up(Acc a, int d) {
+    return comp_f32{__shfl_up_sync(0xffffffffu, a.s, d), __shfl_up_sync(0xffffffffu, a.c, d)};
+  }
+  __device__ __forceinline__ static Acc shfl_down(Acc a, int d) {
+    return comp_f32{__shfl_down_sync(0xffffffffu, a.s, d), __shfl_down_sync(0xffffffffu, a.c, d)};
+  }
+  __device__ __forceinline__ static Acc shfl(Acc a, int s) {
+    return comp_f32{__shfl_sync(0xffffffffu, a.s, s), __shfl_sync(0xffffffffu, a.c, s)};
+  }
+};
+
+// (head flag | run count, value) triple and its order-preserving combine.
+template <class P>
+struct Seg {
+  uint32_t c;  // kHeadBit | count of heads
+  typename P::Acc v;
+};
+template <class P>
+__device__ __forceinline__ Seg<P> seg_comb(const Seg<P> &a, const Seg<P> &b) {
+  Seg<P> r;
+  r.c = ((a.c & kCountMask) + (b.c & kCountMask)) | ((a.c | b.c) & kHeadBit);
+  r.v = (b.c & kHeadBit) ? b.v : P::comb(a.v, b.v);
+  return r;
+}
+template <class P>
+__device__ __forceinline__ Seg<P> seg_ident() {
+  return Seg<P>{0u, P::ident()};
+}
+
+template <class P>
+struct RbStatus {
+  uint32_t *flags;
+  Seg<P> *agg;
+  Seg<P> *inc;
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, const Seg<P> &s) {
+    if (flag == kRbAggregate) agg[t] = s;
+    else inc[t] = s;
+    st_release_u32(&flags[t], flag);
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, Seg<P> *s) const {
+    uint32_t f = ld_acquire_u32(&flags[t]);
+    if (f != kRbInvalid) {
+      const Seg<P> *src = (f == kRbAggregate) ? &agg[t] : &inc[t];
+      const volatile uint32_t *w = reinterpret_cast<const volatile uint32_t *>(src);
+      uint32_t tmp[sizeof(Seg<P>) / 4];
+#pragma unroll
+      for (int i = 0; i < int(sizeof(Seg<P>) / 4); ++i) tmp[i] = w[i];
+      memcpy(s, tmp, sizeof(Seg<P>));
+    }
+    return f;
+  }
+};
+
+template <class K>
+__device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
+
+template <class K, class V, class P>
+__global__ void __launch_bounds__(kRbkThreads)
+reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uint32_t n,
+                     K *__restrict__ keys_out, V *__restrict__ vals_out,
+                     unsigned long long *__restrict__ num_runs, RbStatus<P> st,
+                     uint32_t *__restrict__ tile_counter, int single, uint32_t *err) {
+  typedef Seg<P> S;
+  __shared__ S s_warp[kRbkWarps];
+  __shared__ S s_prefix;
+  __shared__ uint32_t s_tile;
+  const unsigned lane = lane_id(), warp = threadIdx.x / kWarp;
+  uint32_t tile = 0;
+  if (!single) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+    __syncthreads();
+    tile = s_tile;
+  }
+  const uint32_t warp_base = tile * kRbkTile + warp * (kWarp * kRbkItems);
+
+  K k[kRbkItems];
+  V v[kRbkItems];
+#pragma unroll
+  for (int i = 0; i < kRbkItems; ++i) {
+    const uint32_t idx = warp_base + i * kWarp + lane;
+    if (idx < n) {
+      k[i] = keys[idx];
+      v[i] = vals[idx];
+    } else {
+      k[i] = K(0);
+      v[i] = V(0);
+    }
+  }
+  // Head flags: previous element is lane-1 of the same item, lane 31 of the
+  // previous item, or (item 0, lane 0) the element before this warp's run.
+  uint32_t head_mask = 0;  // bit i = element of item i is a run head
+  const K before = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);
+#pragma unroll
+  for (int i = 0; i < kRbkItems; ++i) {
+    const uint32_t idx = warp_base + i * kWarp + lane;
+    K prev = __shfl_up_sync(0xffffffffu, k[i], 1);
+    const K last_prev_item = __shfl_sync(0xffffffffu, k[i > 0 ? i - 1 : 0], kWarp - 1);
+    if (lane == 0) prev = (i > 0) ? last_prev_item : before;
+    const bool h = (idx < n) && (idx == 0 || !keys_equal(prev, k[i]));
+    head_mask |= uint32_t(h) << i;
+  }
+  // Per item: warp inclusive segmented scan (lane_incl), carried across items.
+  S lane_incl[kRbkItems];
+  S run = seg_ident<P>();
+#pragma unroll
+  for (int i = 0; i < kRbkItems; ++i) {
+    const uint32_t idx = warp_base + i * kWarp + lane;
+    S x;
+    const bool h = (head_mask >> i) & 1u;
+    x.c = h ? (kHeadBit | 1u) : 0u;
+    x.v = (idx < n) ? P::from(v[i]) : P::ident();
+#pragma unroll
+    for (int d = 1; d < kWarp; d <<= 1) {
+      S o;
+      o.c = __shfl_up_sync(0xffffffffu, x.c, d);
+      o.v = P::shfl_up(x.v, d);
+      if (int(lane) >= d) x = seg_comb<P>(o, x);
+    }
+    lane_incl[i] = x;
+    S tot;
+    tot.c = __shfl_sync(0xffffffffu, x.c, kWarp - 1);
+    tot.v = P::shfl(x.v, kWarp - 1);
+    run = seg_comb<P>(run, tot);
+  }
+  if (lane == 0) s_warp[warp] = run;
+  __syncthreads();
+  S warp_excl = seg_ident<P>(), tile_agg = seg_ident<P>();
+#pragma unroll
+  for (int w = 0; w < kRbkWarps; ++w) {
+    if (w == int(warp)) warp_excl = tile_agg;
+    tile_agg = seg_comb<P>(tile_agg, s_warp[w]);
+  }
+  if (single) {
+    if (threadIdx.x == 0) s_prefix = seg_ident<P>();
+  } else if (warp == 0) {
+    S excl = seg_ident<P>();
+    if (tile == 0) {
+      if (lane == 0) st.publish(0, kRbPrefix, tile_agg);
+    } else {
+      if (lane == 0) st.publish(tile, kRbAggregate, tile_agg);
+      int64_t pred = int64_t(tile) - 1;
+      bool gave_up = false;
+      while (true) {
+        const int64_t t = pred - int64_t(lane);
+        S val = seg_ident<P>();
+        uint32_t f = kRbPrefix;
+        if (t >= 0) {
+          uint32_t spins = 0;
+          f = st.poll(size_t(t), &val);
+          while (f == kRbInvalid) {
+            if (++spins > kSpinLimit) {
+              gave_up = true;
+              f = kRbPrefix;
+              val = seg_ident<P>();
+              break;
+            }
+            __nanosleep(spins < 64 ? 32 : 256);
+            f = st.poll(size_t(t), &val);
+          }
+        }
+        const unsigned pmask = __ballot_sync(0xffffffffu, f == kRbPrefix);
+        const int first = pmask ? __ffs(pmask) - 1 : kWarp - 1;
+        if (int(lane) > first) val = seg_ident<P>();
+        // Order-preserving fold: higher lanes are earlier tiles.
+#pragma unroll
+        for (int d = 1; d < kWarp; d <<= 1) {
+          S o;
+          o.c = __shfl_down_sync(0xffffffffu, val.c, d);
+          o.v = P::shfl_down(val.v, d);
+          if (int(lane) + d < kWarp) val = seg_comb<P>(o, val);
+        }
+        S window;
+        window.c = __shfl_sync(0xffffffffu, val.c, 0);
+        window.v = P::shfl(val.v, 0);
+        excl = seg_comb<P>(window, excl);
+        if (pmask) break;
+        pred -= kWarp;
+      }
+      if (__any_sync(0xffffffffu, gave_up) && lane == 0) report_error(err, kErrLookbackTimeout);
+      if (lane == 0) st.publish(tile, kRbPrefix, seg_comb<P>(excl, tile_agg));
+    }
+    if (lane == 0) s_prefix = excl;
+  }
+  __syncthreads();
+  // Emit: heads write keys, run ends write values.
+  S pre = seg_comb<P>(s_prefix, warp_excl);
+#pragma unroll
+  for (int i = 0; i < kRbkItems; ++i) {
+    const uint32_t idx = warp_base + i * kWarp + lane;
+    const S incl = seg_comb<P>(pre, lane_incl[i]);
+    const bool h = (head_mask >> i) & 1u;
+    // next element's head flag
+    bool next_head = __shfl_down_sync(0xffffffffu, h ? 1u : 0u, 1) != 0;
+    const uint32_t next_item_h0 = __shfl_sync(0xffffffffu, (head_mask >> (i + 1 < kRbkItems ? i + 1 : i)) & 1u, 0);
+    if (lane == kWarp - 1) {
+      if (i + 1 < kRbkItems) next_head = next_item_h0 != 0;
+      else next_head = (idx + 1 < n) ? !keys_equal(keys[idx + 1], k[i]) : true;
+    }
+    if (idx < n) {
+      const uint32_t run_idx = (incl.c & kCountMask) - 1u;
+      if (h) keys_out[run_idx] = k[i];
+      if (idx + 1 == n || next_head) vals_out[run_idx] = P::out(incl.v);
+      if (idx + 1 == n) *num_runs = (unsigned long long)(incl.c & kCountMask);
+    }
+    S tot;
+    tot.c = __shfl_sync(0xffffffffu, lane_incl[i].c, kWarp - 1);
+    tot.v = P::shfl(lane_incl[i].v, kWarp - 1);
+    pre = seg_comb<P>(pre, tot);
+  }
+}
+
+template <class K, class V, class P>
+bcx_status run_rbk(cudaStream_t s, const void *keys, const void *vals, size_t n, void *keys_out,
+                   void *vals_out, uint64_t *num_runs, void *temp, size_t *temp_bytes) {
+  typedef Seg<P> S;
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
+  const size_t tiles = div_up(n, kRbkTile);
+  const bool single = tiles <= 1;
+  const size_t need = single ? 0 : 256 + align256(tiles * 4) + 2 * align256(tiles * sizeof(S));
+  TempStorage ts;
+  bool query = false;
+  rc = ts.acquire(temp, temp_bytes, need, s, &query);
+  if (rc || query) return rc;
+  RbStatus<P> st{nullptr, nullptr, nullptr};
+  uint32_t *counter = nullptr;
+  if (!single) {
+    char *base = static_cast<char *>(ts.ptr());
+    counter = reinterpret_cast<uint32_t *>(base);
+    st.flags = reinterpret_cast<uint32_t *>(base + 256);
+    st.agg = reinterpret_cast<S *>(base + 256 + align256(tiles * 4));
+    st.inc = reinterpret_cast<S *>(base + 256 + align256(tiles * 4) + align256(tiles * sizeof(S)));
+    BCX_CUDA(cudaMemsetAsync(base, 0, 256 + align256(tiles * 4), s));
+  }
+  KernelScope ks("reduce_by_key", s);
+  reduce_by_key_kernel<K, V, P><<<unsigned(tiles), kRbkThreads, 0, s>>>(
+      static_cast<const K *>(keys), static_cast<const V *>(vals), uint32_t(n), static_cast<K *>(keys_out),
+      static_cast<V *>(vals_out), reinterpret_cast<unsigned long long *>(num_runs), st, counter,
+      single ? 1 : 0, ds->err_word);
+  return launch_status("reduce_by_key");
+}
+
+template <class K, class V>
+bcx_status rbk_op(cudaStream_t s, int op, int comp, const void *k, const void *v, size_t n, void *ko,
+                  void *vo, uint64_t *nr, void *temp, size_t *tb) {
+  switch (op) {
+    case BCX_PLUS:
+      if constexpr (sizeof(V) == 4 && type_traits<V>::is_float) {
+        if (comp) return run_rbk<K, V, RbCompF32>(s, k, v, n, ko, vo, nr, temp, tb);
+      }
+      return run_rbk<K, V, RbPlain<V, op_plus>>(s, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_MULTIPLIES: return run_rbk<K, V, RbPlain<V, op_multiplies>>(s, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_MIN: return run_rbk<K, V, RbPlain<V, op_min>>(s, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_MAX: return run_rbk<K, V, RbPlain<V, op_max>>(s, k, v, n, ko, vo, nr, temp, tb);
+  }
+  return BCX_UNSUPPORTED;
+}
+
+template <class K>
+bcx_status rbk_val(cudaStream_t s, bcx_dtype vt, int op, int comp, const void *k, const void *v, size_t n,
+                   void *ko, void *vo, uint64_t *nr, void *temp, size_t *tb) {
+  switch (vt) {
+    case BCX_INT: return rbk_op<K, int32_t>(s, op, comp, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_UINT: return rbk_op<K, uint32_t>(s, op, comp, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_LONG: return rbk_op<K, long long>(s, op, comp, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_ULONG: return rbk_op<K, unsigned long long>(s, op, comp, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_FLOAT: return rbk_op<K, float>(s, op, comp, k, v, n, ko, vo, nr, temp, tb);
+    case BCX_DOUBLE: return rbk_op<K, double>(s, op, comp, k, v, n, ko, vo, nr, temp, tb);
+    default: break;
+  }
+  return BCX_UNSUPPORTED;
+}
+
+}  // namespace
+}  // namespace bcx
+
+extern "C" bcx_status bcx_reduce_by_key(bcx_stream stream, bcx_dtype key_type, bcx_dtype value_type,
+                                        bcx_op op, const void *keys_in, const void *values_in, size_t n,
+                                        void *keys_out, void *values_out, uint64_t *num_runs_dev,
+                                        int compensated, void *temp, size_t *temp_bytes) {
+  using namespace bcx;
+  clear_error();
+  BCX_CHECK(dtype_valid(key_type) && dtype_valid(value_type), BCX_INVALID_VALUE, "invalid dtype");
+  BCX_CHECK(n < (size_t(1) << 31), BCX_INVALID_VALUE, "reduce_by_key: n must be below 2^31");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n == 0) {
+    if (temp == nullptr && temp_bytes != nullptr) {
+      *temp_bytes = 0;
+      return BCX_SUCCESS;
+    }
+    if (num_runs_dev) BCX_CUDA(cudaMemsetAsync(num_runs_dev, 0, sizeof(uint64_t), s));
+    return BCX_SUCCESS;
+  }
+  BCX_CHECK(keys_in && values_in && keys_out && values_out && num_runs_dev, BCX_INVALID_VALUE,
+            "NULL argument");
+  bcx_status rc = BCX_UNSUPPORTED;
+  switch (key_type) {
+    case BCX_INT: rc = rbk_val<int32_t>(s, value_type, op, compensated, keys_in, values_in, n, keys_out, values_out, num_runs_dev, temp, temp_bytes); break;
+    case BCX_UINT: rc = rbk_val<uint32_t>(s, value_type, op, compensated, keys_in, values_in, n, keys_out, values_out, num_runs_dev, temp, temp_bytes); break;
+    case BCX_LONG: rc = rbk_val<long long>(s, value_type, op, compensated, keys_in, values_in, n, keys_out, values_out, num_runs_dev, temp, temp_bytes); break;
+    case BCX_ULONG: rc = rbk_val<unsigned long long>(s, value_type, op, compensated, keys_in, values_in, n, keys_out, values_out, num_runs_dev, temp, temp_bytes); break;
+    case BCX_FLOAT: rc = rbk_val<float>(s, value_type, op, compensated, keys_in, values_in, n, keys_out, values_out, num_runs_dev, temp, temp_bytes); break;
+    default: break;
+  }
+  if (rc == BCX_UNSUPPORTED)
+    set_error("reduce_by_key: key dtype %d / value dtype %d / functor %d not provided", int(key_type),
+              int(value_type), int(op));
+  return rc;
+}

@@ -318,13 +318,15 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
     if (w == int(warp)) warp_excl = tile_agg;
     tile_agg = P::comb(tile_agg, warp_tot[w]);
   }
+  // Tile 0 starts from init (exclusive) or the functor's identity (inclusive).
+  const Carry first_prefix = exclusive ? init_carry : P::carry_ident();
   if (SINGLE) {
-    if (threadIdx.x == 0) tile_prefix = init_carry;
+    if (threadIdx.x == 0) tile_prefix = first_prefix;
   } else if (warp == 0) {
     Carry pre;
     if (tile == 0) {
-      pre = init_carry;
-      if (lane == 0) st.publish(0, kFlagPrefix, P::carry_comb(init_carry, P::to_carry(tile_agg)));
+      pre = first_prefix;
+      if (lane == 0) st.publish(0, kFlagPrefix, P::carry_comb(first_prefix, P::to_carry(tile_agg)));
     } else {
       pre = lookback<P>(st, tile, P::to_carry(tile_agg), err);
     }

@@ -85,35 +85,56 @@ struct SortControl {
 static_assert(sizeof(SortControl) == 256, "control block is 256 bytes");
 
 // ---------------------------------------------------------------------------
-// 1. Histogram of every digit position, one read of the keys.
+// 1. Histogram of every digit position, one read of the keys.  Keys stream in
+// as 16-byte vectors; a warp whose 32 keys are identical adds 32 once per
+// digit position instead of 32 shared-memory atomics on one address (the
+// all-equal and heavily skewed distributions).
+template <class U, int PASSES>
+__device__ __forceinline__ void hist_count(uint32_t (*sh)[kRadix], U k, bool valid, unsigned lane) {
+  const U k0 = __shfl_sync(0xffffffffu, k, 0);
+  if (__all_sync(0xffffffffu, valid && k == k0)) {
+    if (lane == 0) {
+#pragma unroll
+      for (int p = 0; p < PASSES; ++p) atomicAdd(&sh[p][uint32_t(k0 >> (p * kRadixBits)) & (kRadix - 1)], 32u);
+    }
+  } else if (valid) {
+#pragma unroll
+    for (int p = 0; p < PASSES; ++p) atomicAdd(&sh[p][uint32_t(k >> (p * kRadixBits)) & (kRadix - 1)], 1u);
+  }
+}
+
 template <class U, int PASSES>
 __global__ void __launch_bounds__(kHistThreads)
-radix_histogram_kernel(const U *__restrict__ keys, size_t n, int kind, int desc,
+radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t nvec, int kind, int desc,
                        uint32_t *__restrict__ hist) {
+  constexpr int N = 16 / sizeof(U);
   __shared__ uint32_t sh[PASSES][kRadix];
   for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
   __syncthreads();
-  const size_t gtid = size_t(blockIdx.x) * kHistThreads + threadIdx.x;
-  const size_t stride = size_t(gridDim.x) * kHistThreads;
   const unsigned lane = lane_id();
-  // Every lane of a warp runs the same number of iterations so that the
-  // warp-uniform shortcut can use full-warp votes.
-  const size_t warp_first = gtid - lane;
-  for (size_t base = warp_first; base < n; base += stride) {
-    const size_t i = base + lane;
-    const bool valid = i < n;
-    U k = valid ? radix_key_rt<U>(keys[i], kind, desc) : U(0);
-    const bool full = __all_sync(0xffffffffu, valid);
-#pragma unroll
-    for (int p = 0; p < PASSES; ++p) {
-      const uint32_t d = uint32_t(k >> (p * kRadixBits)) & (kRadix - 1);
-      const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
-      if (full && __all_sync(0xffffffffu, d == d0)) {
-        if (lane == 0) atomicAdd(&sh[p][d0], 32u);
-      } else if (valid) {
-        atomicAdd(&sh[p][d], 1u);
-      }
+  const size_t warp_id = (size_t(blockIdx.x) * kHistThreads + threadIdx.x) / kWarp;
+  const size_t nwarps = size_t(gridDim.x) * kHistThreads / kWarp;
+  // Unaligned head and the tail: the first warp, 32 scalars at a time.
+  if (warp_id == 0) {
+    const size_t tail = head + nvec * N;
+    for (size_t b = 0; b < head; b += kWarp) {
+      const bool valid = b + lane < head;
+      hist_count<U, PASSES>(sh, valid ? radix_key_rt<U>(keys[b + lane], kind, desc) : U(0), valid, lane);
     }
+    for (size_t b = tail; b < n; b += kWarp) {
+      const bool valid = b + lane < n;
+      hist_count<U, PASSES>(sh, valid ? radix_key_rt<U>(keys[b + lane], kind, desc) : U(0), valid, lane);
+    }
+  }
+  const vec16<U> *vk = reinterpret_cast<const vec16<U> *>(keys + head);
+  for (size_t vb = warp_id * kWarp; vb < nvec; vb += nwarps * kWarp) {
+    const size_t v = vb + lane;
+    const bool valid = v < nvec;
+    vec16<U> r;
+    if (valid) r = ld_stream16(vk + v);
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+      hist_count<U, PASSES>(sh, valid ? radix_key_rt<U>(r.v[j], kind, desc) : U(0), valid, lane);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) {
@@ -431,11 +452,17 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
   BCX_CUDA(cudaMemsetAsync(base + L.zero_begin, 0, L.zero_bytes, s));
   {
     KernelScope ks("radix_histogram", s);
-    size_t blocks = div_up(n, size_t(kHistThreads) * 16);
-    size_t cap = size_t(ds->sm_count) * 4;
+    constexpr int N = 16 / sizeof(U);
+    const uintptr_t a = reinterpret_cast<uintptr_t>(keys);
+    size_t head = (a % sizeof(U)) ? n : ((16u - (a & 15u)) & 15u) / sizeof(U);
+    if (head > n) head = n;
+    const size_t nvec = (n - head) / N;
+    size_t blocks = div_up(nvec, size_t(kHistThreads) * 4);
+    size_t cap = size_t(ds->sm_count) * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    radix_histogram_kernel<U, PASSES><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, kind, desc, hist);
+    radix_histogram_kernel<U, PASSES><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, kind,
+                                                                                 desc, hist);
     rc = launch_status("radix_histogram");
     if (rc) return rc;
   }

@@ -180,6 +180,20 @@ bcx_status bcx_transform_binary(bcx_stream stream, bcx_dtype type, bcx_op op,
 bcx_status bcx_transform_saxpy(bcx_stream stream, bcx_dtype type, const void *alpha,
                                const void *x, const void *y, void *out, size_t n);
 
+/* ---- reduce_by_key -------------------------------------------------------
+ * reduce_by_key(keys, keys+n, values, keys_out, values_out, op, equal_to)
+ * (reduce_by_key.hpp, detail/reduce_by_key_with_scan.hpp:432-486): one output
+ * per run of equal consecutive keys; the run count goes to *num_runs_dev
+ * (a device uint64).  Key types int/uint/long/ulong/float (typed ==);
+ * value types int/uint/long/ulong/float/double; functors plus, multiplies,
+ * min, max.  compensated = 1 with float plus keeps Neumaier pairs. */
+bcx_status bcx_reduce_by_key(bcx_stream stream, bcx_dtype key_type,
+                             bcx_dtype value_type, bcx_op op,
+                             const void *keys_in, const void *values_in, size_t n,
+                             void *keys_out, void *values_out,
+                             uint64_t *num_runs_dev, int compensated,
+                             void *temp, size_t *temp_bytes);
+
 /* ---- profiling (command_queue::enable_profiling / event::duration,
  *      command_queue.hpp:82, event.hpp:269) --------------------------------
  * When enabled, every kernel this library launches is bracketed by CUDA

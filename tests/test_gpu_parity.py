@@ -410,3 +410,67 @@ def test_scan_reduce_2p28_consistency(bc, cuda):
 
 def test_device_error_word_clean(bc, cuda):
     bc.device_error_check()
+
+
+# ---- reduce_by_key ----------------------------------------------------------
+RBK_CASES = cases("reduce_by_key")
+
+
+@pytest.mark.parametrize("case", RBK_CASES, ids=ids(RBK_CASES))
+def test_reduce_by_key_golden(bc, cuda, case):
+    kt, vt = case["dtype"], case["value_dtype"]
+    ko, vo = bc.reduce_by_key(to_dev(cuda, arr(case["inputs"][0], kt), kt),
+                              to_dev(cuda, arr(case["inputs"][1], vt), vt), op=case["op"])
+    np.testing.assert_array_equal(to_np(ko, kt), arr(case["expected"][0], kt))
+    np.testing.assert_array_equal(to_np(vo, vt), arr(case["expected"][1], vt))
+
+
+def test_reduce_by_key_long_vector_golden(bc, cuda):
+    # test/test_reduce_by_key.cpp:48-73
+    keys = cuda.zeros(1024, dtype=cuda.int32, device="cuda")
+    ko, vo = bc.reduce_by_key(keys, cuda.ones(1024, dtype=cuda.int32, device="cuda"))
+    assert ko.tolist() == [0] and vo.tolist() == [1024]
+    keys[[137, 677, 1001]] = 1
+    keys = bc.inclusive_scan(keys)
+    ko, vo = bc.reduce_by_key(keys, cuda.ones(1024, dtype=cuda.int32, device="cuda"))
+    assert ko.tolist() == [0, 1, 2, 3] and vo.tolist() == [137, 540, 324, 23]
+
+
+def test_reduce_by_key_empty(bc, cuda):
+    ko, vo = bc.reduce_by_key(cuda.empty(0, dtype=cuda.int32, device="cuda"),
+                              cuda.empty(0, dtype=cuda.int32, device="cuda"))
+    assert ko.numel() == 0 and vo.numel() == 0
+
+
+@pytest.mark.parametrize("kt,vt,op", [("int", "int", "plus"), ("uint", "long", "plus"), ("int", "int", "min"),
+                                      ("long", "int", "max"), ("int", "uint", "multiplies"),
+                                      ("float", "int", "plus"), ("ulong", "ulong", "plus")])
+def test_reduce_by_key_random(bc, cuda, kt, vt, op):
+    rng = np.random.default_rng(17)
+    for n, mean_run in [(1, 1), (100, 3), (2049, 1), (70_001, 40), (1_000_003, 5000), (300_000, 1)]:
+        runs = np.maximum(1, rng.geometric(1.0 / mean_run, size=n)).cumsum()
+        keys = np.searchsorted(runs, np.arange(n), side="right")
+        keys = (keys * 7 % 1000).astype(NP[kt])  # adjacent runs may share a key value
+        vals = random_keys(rng, vt, n)
+        if op == "multiplies":
+            vals = rng.integers(1, 3, size=n).astype(NP[vt])
+        ko, vo = bc.reduce_by_key(to_dev(cuda, keys, kt), to_dev(cuda, vals, vt), op=op,
+                                  key_dtype=kt, value_dtype=vt)
+        rk, rv = oracle.reduce_by_key(keys, vals, kt, vt, op=op)
+        np.testing.assert_array_equal(to_np(ko, kt), rk, err_msg=f"n={n}")
+        np.testing.assert_array_equal(to_np(vo, vt), rv, err_msg=f"n={n}")
+
+
+def test_reduce_by_key_float_segments(bc, cuda):
+    """reduce_by_key float32 N(0,1) with keys = segment ids: each segment sum
+    within 2 ulp of its magnitude-scaled FP64 value (compensated pairs)."""
+    rng = np.random.default_rng(23)
+    sizes = np.exp(rng.uniform(np.log(16), np.log(1 << 14), size=400)).astype(np.int64)
+    keys = np.repeat(np.arange(sizes.size, dtype=np.int32), sizes)
+    vals = rng.standard_normal(keys.size).astype(np.float32)
+    ko, vo = bc.reduce_by_key(to_dev(cuda, keys, "int"), to_dev(cuda, vals, "float"))
+    rk, rv = oracle.reduce_by_key(keys, vals, "int", "float")
+    np.testing.assert_array_equal(to_np(ko, "int"), rk)
+    got = to_np(vo, "float").astype(np.float64)
+    bound = np.array([np.abs(vals[keys == i]).sum() for i in range(sizes.size)]) * 2.0 ** -23 * 2
+    assert (np.abs(got - rv.astype(np.float64)) <= bound + 1e-30).all()
