@@ -33,8 +33,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "sort Gkeys/s, scan/reduce GB/s vs HBM peak; batched p50/p99 vs plain, 1 GB300"
-N_SORT = 1 << 28
-N_SCAN = 1 << 30
+N_SORT = DEFAULT_N_SORT = 1 << 28
+N_SCAN = DEFAULT_N_SCAN = 1 << 30
 N_SAXPY = 1 << 28
 WORKLOAD = ("sort_by_key uint32 keys (uniform 32-bit) with uint32 values (iota), n=2^28; "
             "also exclusive_scan/reduce int32 n=2^30 and saxpy float32 n=2^28")
@@ -209,8 +209,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all", choices=["all", "sort", "prims"],
                     help="'sort' skips the other primitives, 'prims' skips the sort (profiling runs)")
-    ap.add_argument("--n-sort", type=int, default=N_SORT, help="pairs per sort (default 2^28)")
-    ap.add_argument("--n-scan", type=int, default=N_SCAN, help="scan/reduce elements (default 2^30)")
+    ap.add_argument("--n-sort", type=int, default=DEFAULT_N_SORT, help="pairs per sort (default 2^28)")
+    ap.add_argument("--n-scan", type=int, default=DEFAULT_N_SCAN, help="scan/reduce elements (default 2^30)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1,0 +1,10 @@
+// boost/compute/algorithm.hpp -- every algorithm of the drop-in layer.
+#ifndef BOOST_COMPUTE_ALGORITHM_HPP
+#define BOOST_COMPUTE_ALGORITHM_HPP
+#include <boost/compute/algorithm/copy.hpp>
+#include <boost/compute/algorithm/reduce.hpp>
+#include <boost/compute/algorithm/reduce_by_key.hpp>
+#include <boost/compute/algorithm/scan.hpp>
+#include <boost/compute/algorithm/sort.hpp>
+#include <boost/compute/algorithm/transform.hpp>
+#endif

@@ -1,0 +1,1 @@
+#include <boost/compute/algorithm/copy.hpp>

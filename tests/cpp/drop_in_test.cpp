@@ -1,0 +1,197 @@
+// Drop-in check: reference-style C++ callers compiled unchanged (apart from
+// include paths) against the boost::compute headers of this repository and run
+// on the GPU.  Each CHECK mirrors a known-answer test of the reference's test
+// suite (file:line given); the program prints one line per failure and exits
+// non-zero if any check failed.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <numeric>
+#include <random>
+#include <vector>
+
+#include <boost/compute.hpp>
+
+namespace compute = boost::compute;
+
+static int g_failures = 0;
+#define CHECK(cond)                                                   \
+  do {                                                                \
+    if (!(cond)) {                                                    \
+      std::printf("FAIL %s:%d: %s\n", __FILE__, __LINE__, #cond);     \
+      ++g_failures;                                                   \
+    }                                                                 \
+  } while (0)
+
+template <class T>
+static std::vector<T> to_host(const compute::vector<T> &v, compute::command_queue &q) {
+  std::vector<T> h(v.size());
+  compute::copy(v.begin(), v.end(), h.begin(), q);
+  return h;
+}
+
+// The README example: sort 2^20 random floats on the device.
+static void readme_example() {
+  compute::device gpu = compute::system::default_device();
+  compute::context ctx(gpu);
+  compute::command_queue queue(ctx, gpu);
+  std::vector<float> host_vector(1 << 20);
+  std::mt19937 gen(20261203);
+  for (auto &x : host_vector) x = float(gen() % 2147483647u);
+  compute::vector<float> device_vector(host_vector.size(), ctx);
+  compute::copy(host_vector.begin(), host_vector.end(), device_vector.begin(), queue);
+  compute::sort(device_vector.begin(), device_vector.end(), queue);
+  std::vector<float> sorted(host_vector.size());
+  compute::copy(device_vector.begin(), device_vector.end(), sorted.begin(), queue);
+  std::vector<float> expect = host_vector;
+  std::sort(expect.begin(), expect.end());
+  CHECK(sorted == expect);
+}
+
+static void sort_cases(compute::command_queue &q) {
+  // test/test_sort.cpp:135-145
+  int data[] = {-4, 152, -5000, 963, 75321, -456, 0, 1112};
+  compute::vector<int> v(data, data + 8, q);
+  CHECK(!compute::is_sorted(v.begin(), v.end(), q));
+  compute::sort(v.begin(), v.end(), q);
+  CHECK((to_host(v, q) == std::vector<int>{-5000, -456, -4, 0, 152, 963, 1112, 75321}));
+  // test/test_sort.cpp:227-236 (greater)
+  compute::vector<int> r(data, data + 8, q);
+  compute::sort(r.begin(), r.end(), compute::greater<int>(), q);
+  CHECK((to_host(r, q) == std::vector<int>{75321, 1112, 963, 152, 0, -4, -456, -5000}));
+  // test/test_sort.cpp:286-292 (host vector)
+  std::vector<int> hv = {5, 2, 3, 6, 7, 4, 0, 1};
+  compute::sort(hv.begin(), hv.end(), q);
+  CHECK((hv == std::vector<int>{0, 1, 2, 3, 4, 5, 6, 7}));
+  // test/test_radix_sort.cpp:530-543 (sub-range)
+  int d2[] = {9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
+  compute::vector<int> p(d2, d2 + 10, q);
+  compute::detail::radix_sort(p.begin() + 2, p.end() - 2, q);
+  CHECK((to_host(p, q) == std::vector<int>{9, 8, 2, 3, 4, 5, 6, 7, 1, 0}));
+  // test/test_radix_sort_by_key.cpp:30-61 (stability)
+  int keys[] = {10, 9, 2, 7, 6, -1, 4, 2, 2, 10};
+  int vals[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10};
+  compute::vector<int> k(keys, keys + 10, q), w(vals, vals + 10, q);
+  compute::sort_by_key(k.begin(), k.end(), w.begin(), q);
+  CHECK((to_host(k, q) == std::vector<int>{-1, 2, 2, 2, 4, 6, 7, 9, 10, 10}));
+  CHECK((to_host(w, q) == std::vector<int>{6, 3, 8, 9, 7, 5, 4, 2, 1, 10}));
+  // large stable sort_by_key
+  const size_t n = 1000003;
+  std::vector<compute::uint_> hk(n), hvals(n);
+  std::mt19937 gen(1);
+  for (size_t i = 0; i < n; ++i) { hk[i] = gen() % 1000; hvals[i] = compute::uint_(i); }
+  compute::vector<compute::uint_> dk(hk.begin(), hk.end(), q), dv(hvals.begin(), hvals.end(), q);
+  compute::stable_sort_by_key(dk.begin(), dk.end(), dv.begin(), q);
+  std::vector<size_t> idx(n);
+  std::iota(idx.begin(), idx.end(), size_t(0));
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return hk[a] < hk[b]; });
+  std::vector<compute::uint_> gk = to_host(dk, q), gv = to_host(dv, q);
+  bool ok = true;
+  for (size_t i = 0; i < n; ++i) ok = ok && gk[i] == hk[idx[i]] && gv[i] == compute::uint_(idx[i]);
+  CHECK(ok);
+}
+
+static void scan_cases(compute::command_queue &q) {
+  // test/test_scan.cpp:41-60 / 91-110
+  int data[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11};
+  compute::vector<int> v(data, data + 12, q), out(12, q.get_context());
+  compute::inclusive_scan(v.begin(), v.end(), out.begin(), q);
+  CHECK((to_host(out, q) == std::vector<int>{0, 1, 3, 6, 10, 15, 21, 28, 36, 45, 55, 66}));
+  compute::exclusive_scan(v.begin(), v.end(), v.begin(), q);  // in place
+  CHECK((to_host(v, q) == std::vector<int>{0, 0, 1, 3, 6, 10, 15, 21, 28, 36, 45, 55}));
+  // test/test_scan.cpp:360-390 (multiplies, init 10)
+  int m[] = {1, 2, 1, 2, 3};
+  compute::vector<int> mv(m, m + 5, q), mo(5, q.get_context());
+  compute::exclusive_scan(mv.begin(), mv.end(), mo.begin(), 10, compute::multiplies<int>(), q);
+  CHECK((to_host(mo, q) == std::vector<int>{10, 10, 20, 20, 40}));
+  // test/test_scan.cpp:190-222 (counting iterator input)
+  compute::vector<int> c(10, q.get_context());
+  compute::inclusive_scan(compute::make_counting_iterator(1), compute::make_counting_iterator(11), c.begin(), q);
+  CHECK((to_host(c, q) == std::vector<int>{1, 3, 6, 10, 15, 21, 28, 36, 45, 55}));
+}
+
+static void reduce_cases(compute::command_queue &q) {
+  // test/test_reduce.cpp:29-40
+  int data[] = {1, 5, 9, 13, 17};
+  compute::vector<int> v(data, data + 5, q);
+  int sum = 0, product = 0;
+  compute::reduce(v.begin(), v.end(), &sum, compute::plus<int>(), q);
+  compute::reduce(v.begin(), v.end(), &product, compute::multiplies<int>(), q);
+  CHECK(sum == 45);
+  CHECK(product == 9945);
+  // test/test_reduce.cpp:80-88 (device result)
+  int d8[] = {1, 2, 3, 4, 5, 6, 7, 8};
+  compute::vector<int> in(d8, d8 + 8, q), res(2, q.get_context());
+  compute::reduce(in.begin(), in.begin() + 4, res.begin(), q);
+  compute::reduce(in.begin() + 4, in.end(), res.end() - 1, q);
+  CHECK((to_host(res, q) == std::vector<int>{10, 26}));
+  // test/test_reduce.cpp:42-49 (empty leaves the result alone)
+  compute::vector<short> empty(q.get_context());
+  short s = 0;
+  compute::reduce(empty.begin(), empty.end(), &s, q);
+  CHECK(s == 0);
+  // test/test_accumulate.cpp:25-85
+  int a[] = {2, 4, 6, 8};
+  compute::vector<int> av(a, a + 4, q);
+  CHECK(compute::accumulate(av.begin(), av.end(), 0, q) == 20);
+  CHECK(compute::accumulate(av.begin(), av.end(), -10, q) == 10);
+  CHECK(compute::accumulate(av.begin(), av.end(), 2, compute::multiplies<int>(), q) == 768);
+  int qd[] = {2, 8, 16};
+  compute::vector<int> qv(qd, qd + 3, q);
+  CHECK(compute::accumulate(qv.begin(), qv.end(), 1024, compute::divides<int>(), q) == 4);
+  // test/test_accumulate.cpp:150-206 (iota sums)
+  compute::vector<int> io(1025, q.get_context());
+  compute::iota(io.begin(), io.end(), 0, q);
+  CHECK(compute::accumulate(io.begin(), io.end(), 2, q) == 524802);
+}
+
+static void transform_cases(compute::command_queue &q) {
+  // test/test_transform.cpp:29-41
+  int data[] = {1, -2, -3, -4, 5};
+  compute::vector<int> v(data, data + 5, q);
+  compute::transform(v.begin(), v.end(), v.begin(), compute::abs<int>(), q);
+  CHECK((to_host(v, q) == std::vector<int>{1, 2, 3, 4, 5}));
+  // test/test_transform.cpp:75-99
+  int d1[] = {1, 2, 3, 4}, d2[] = {10, 20, 30, 40};
+  compute::vector<int> i1(d1, d1 + 4, q), i2(d2, d2 + 4, q), o(4, q.get_context());
+  compute::transform(i1.begin(), i1.end(), i2.begin(), o.begin(), compute::plus<int>(), q);
+  CHECK((to_host(o, q) == std::vector<int>{11, 22, 33, 44}));
+}
+
+static void reduce_by_key_cases(compute::command_queue &q) {
+  // test/test_reduce_by_key.cpp:26-46
+  int keys[] = {0, 2, -3, -3, -3, -3, -3, 4};
+  int data[] = {1, 1, 1, 1, 1, 2, 5, 1};
+  compute::vector<int> ki(keys, keys + 8, q), vi(data, data + 8, q), ko(8, q.get_context()), vo(8, q.get_context());
+  auto ends = compute::reduce_by_key(ki.begin(), ki.end(), vi.begin(), ko.begin(), vo.begin(), q);
+  CHECK(ends.first - ko.begin() == 4);
+  std::vector<int> hk = to_host(ko, q), hv = to_host(vo, q);
+  CHECK((std::vector<int>(hk.begin(), hk.begin() + 4) == std::vector<int>{0, 2, -3, 4}));
+  CHECK((std::vector<int>(hv.begin(), hv.begin() + 4) == std::vector<int>{1, 1, 10, 1}));
+}
+
+static void error_cases(compute::command_queue &q) {
+  // bcx errors surface as opencl_error with the OpenCL status code
+  bool thrown = false;
+  try {
+    compute::detail::check(bcx_scan(q.get(), bcx_dtype(42), BCX_PLUS, 0, nullptr, nullptr, nullptr, 1, 0, nullptr,
+                                    nullptr));
+  } catch (const compute::opencl_error &e) {
+    thrown = e.error_code() == -30;
+  }
+  CHECK(thrown);
+}
+
+int main() {
+  compute::command_queue &q = compute::system::default_queue();
+  readme_example();
+  sort_cases(q);
+  scan_cases(q);
+  reduce_cases(q);
+  transform_cases(q);
+  reduce_by_key_cases(q);
+  error_cases(q);
+  q.check_device_errors();
+  std::printf("%s (%d failures)\n", g_failures ? "FAILED" : "OK", g_failures);
+  return g_failures ? 1 : 0;
+}
