@@ -31,7 +31,7 @@
 namespace bcx {
 namespace {
 
-constexpr int kScanThreads = 256;
+constexpr int kScanThreads = 128;
 constexpr int kScanWarps = kScanThreads / kWarp;
 
 enum : uint32_t { kFlagInvalid = 0, kFlagAggregate = 1, kFlagPrefix = 2 };
@@ -149,10 +149,11 @@ struct TileStatus<Carry, true> {
     uint32_t bits;
     memcpy(&bits, &v, 4);
     unsigned long long w = (static_cast<unsigned long long>(bits) << 32) | flag;
-    st_release_u64(&words[t], w);
+    // Flag and value travel in one 64-bit word, so relaxed ordering suffices.
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(&words[t]), "l"(w) : "memory");
   }
   __device__ __forceinline__ uint32_t poll(size_t t, Carry *v) const {
-    unsigned long long w = ld_acquire_u64(&words[t]);
+    unsigned long long w = ld_relaxed_u64(&words[t]);
     uint32_t bits = uint32_t(w >> 32);
     memcpy(v, &bits, 4);
     return uint32_t(w & 0xffffffffu);
@@ -212,7 +213,7 @@ __device__ __forceinline__ typename P::Carry lookback(Status &st, size_t tile,
           v = P::carry_ident();
           break;
         }
-        __nanosleep(spins < 64 ? 32 : 256);
+        if (spins > 16) __nanosleep(spins < 256 ? 32 : 256);
         f = st.poll(size_t(t), &v);
       }
     }

@@ -180,6 +180,68 @@ radix_prep_kernel(uint32_t *__restrict__ hist, int passes, uint32_t n,
 }
 
 // 3. One onesweep pass over digit `pass`.
+//
+// Order of work inside a tile is chosen so that a tile's inclusive digit
+// prefixes become visible as early as possible (that is what bounds how far
+// successors must look back): load, count digits with shared-memory atomics,
+// publish the counts, look back (each thread one digit, kLookbackWindow
+// predecessor words in flight at a time), publish the inclusive prefix, and
+// only then rank keys stably and scatter them.
+constexpr int kLookbackWindow = 4;
+
+__device__ __forceinline__ void st_relaxed_u32(uint32_t *p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Exclusive prefix of digit `d` over all tiles before `tile`.
+__device__ __forceinline__ uint32_t onesweep_lookback(const uint32_t *__restrict__ status, uint32_t tile,
+                                                      unsigned d, bool *gave_up) {
+  uint32_t excl = 0;
+  int64_t t = int64_t(tile) - 1;
+  while (t >= 0) {
+    uint32_t w[kLookbackWindow];
+#pragma unroll
+    for (int j = 0; j < kLookbackWindow; ++j)
+      w[j] = (t - j >= 0) ? ld_relaxed_u32(status + size_t(t - j) * kRadix + d) : kStPrefix;
+    bool done = false;
+#pragma unroll
+    for (int j = 0; j < kLookbackWindow; ++j) {
+      if (done) break;
+      uint32_t x = w[j];
+      uint32_t spins = 0;
+      while ((x >> kStFlagShift) == 0) {
+        if (++spins > kSpinLimit) {
+          *gave_up = true;
+          return excl;
+        }
+        __nanosleep(spins < 32 ? 16 : 128);
+        x = ld_relaxed_u32(status + size_t(t - j) * kRadix + d);
+      }
+      excl += x & kStValueMask;
+      done = (x >> kStFlagShift) == 2u;
+    }
+    if (done) break;
+    t -= kLookbackWindow;
+  }
+  return excl;
+}
+
+// Shared-memory footprint of one onesweep block: per-warp digit counters,
+// keys and values in load order, the load index and digit of every staged
+// position in digit order.
+template <class U, int VB>
+struct OnesweepSmem {
+  typedef typename value_type_of<VB>::type VT;
+  static constexpr int IPT = items_per_thread<U>::value;
+  static constexpr int TILE = kSortThreads * IPT;
+  static constexpr size_t kCounters = size_t(kSortWarps) * kRadix * 4;
+  static constexpr size_t kKeys = kCounters;
+  static constexpr size_t kVals = kKeys + size_t(TILE) * sizeof(U);
+  static constexpr size_t kPerm = kVals + (VB ? size_t(TILE) * sizeof(VT) : 0);
+  static constexpr size_t kDigit = kPerm + size_t(TILE) * 2;
+  static constexpr size_t kBytes = kDigit + size_t(TILE);
+};
+
 template <class U, int VB>
 __global__ void __launch_bounds__(kSortThreads)
 radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
@@ -188,17 +250,22 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
                       int pass, int kind, int desc, const uint32_t *__restrict__ digit_start,
                       uint32_t *__restrict__ status, uint32_t *__restrict__ tile_counter,
                       const SortControl *__restrict__ ctrl, uint32_t *err) {
-  typedef typename value_type_of<VB>::type VT;
-  constexpr int IPT = items_per_thread<U>::value;
-  constexpr int TILE = kSortThreads * IPT;
+  typedef OnesweepSmem<U, VB> L;
+  typedef typename L::VT VT;
+  constexpr int IPT = L::IPT;
+  constexpr int TILE = L::TILE;
+  static_assert(kSortThreads == kRadix, "one thread per digit");
+  static_assert(TILE <= 65536, "16-bit load indices");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // Shared layout: [warp digit counters][keys staging][values staging]
   uint32_t *wcnt = reinterpret_cast<uint32_t *>(smem_raw);  // [kSortWarps][kRadix]
-  U *s_keys = reinterpret_cast<U *>(smem_raw + kSortWarps * kRadix * 4);
-  VT *s_vals = reinterpret_cast<VT *>(smem_raw + kSortWarps * kRadix * 4 + TILE * sizeof(U));
+  U *s_keys = reinterpret_cast<U *>(smem_raw + L::kKeys);    // load order
+  VT *s_vals = reinterpret_cast<VT *>(smem_raw + L::kVals);  // load order
+  uint16_t *s_perm = reinterpret_cast<uint16_t *>(smem_raw + L::kPerm);  // digit order -> load index
+  uint8_t *s_digit = smem_raw + L::kDigit;                                  // digit order -> digit
+  __shared__ uint32_t s_hist[kRadix];
   __shared__ uint32_t s_local_start[kRadix];
   __shared__ uint32_t s_adj[kRadix];  // global base - local start, per digit
-  __shared__ uint32_t s_warp_sum[kRadix / kWarp];
+  __shared__ uint32_t s_warp_sum[kSortWarps];
   __shared__ uint32_t s_tile;
 
   if (ctrl->skip[pass]) return;
@@ -211,54 +278,104 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
   const unsigned tid = threadIdx.x, lane = lane_id(), warp = tid / kWarp;
   const int shift = pass * kRadixBits;
   for (int i = lane; i < kRadix; i += kWarp) wcnt[warp * kRadix + i] = 0;
+  s_hist[tid] = 0;
   if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint32_t tile_base = tile * uint32_t(TILE);
-  const uint32_t warp_base = tile_base + warp * (kWarp * IPT);
+  const uint32_t warp_first = warp * (kWarp * IPT);  // tile-local index of this warp's first item
 
-  // Load keys (and values) warp-striped: item i of lane l is element
-  // warp_base + i*32 + l, so ranking items in (i, l) order is input order.
-  U key[IPT];
-  VT val[VB ? IPT : 1];
-#pragma unroll
-  for (int i = 0; i < IPT; ++i) {
-    const uint32_t idx = warp_base + i * kWarp + lane;
-    key[i] = idx < n ? src_k[idx] : U(0);
-  }
-  if (VB) {
+  // Load warp-striped (item i of lane l is tile element warp_first + i*32 + l,
+  // so (i, l) order is input order), stage in shared memory in that order,
+  // and count digits.
+  uint32_t dr[IPT];  // digit | rank-within-warp << 8 | invalid << 31
+  {
+    U key[IPT];
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
-      const uint32_t idx = warp_base + i * kWarp + lane;
-      if (idx < n) val[i] = src_v[idx];
+      const uint32_t idx = tile_base + warp_first + i * kWarp + lane;
+      key[i] = idx < n ? src_k[idx] : U(0);
+    }
+    if (VB) {
+      VT val[VB ? IPT : 1];
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) {
+        const uint32_t idx = tile_base + warp_first + i * kWarp + lane;
+        if (idx < n) val[i] = src_v[idx];
+      }
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) s_vals[warp_first + i * kWarp + lane] = val[i];
+    }
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      const uint32_t li = warp_first + i * kWarp + lane;
+      s_keys[li] = key[i];
+      if (tile_base + li < n) {
+        dr[i] = uint32_t(radix_key_rt<U>(key[i], kind, desc) >> shift) & (kRadix - 1);
+        atomicAdd(&s_hist[dr[i]], 1u);
+      } else {
+        dr[i] = 0x80000000u;
+      }
     }
   }
+  __syncthreads();
 
-  // Rank: per item, lanes with equal digits form a match group; the group's
-  // lowest lane advances the warp's counter for that digit.
-  uint32_t dr[IPT];  // digit | rank-within-warp << 8 | invalid << 31
+  // Thread `tid` owns digit `tid`: publish, local start, look-back.
+  const uint32_t tile_cnt = s_hist[tid];
+  uint32_t *my_status = status + size_t(tile) * kRadix + tid;
+  st_relaxed_u32(my_status, (tile == 0 ? kStPrefix : kStAggregate) | tile_cnt);
+  uint32_t incl = tile_cnt;
+#pragma unroll
+  for (int o = 1; o < kWarp; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (int(lane) >= o) incl += t;
+  }
+  if (lane == kWarp - 1) s_warp_sum[warp] = incl;
+  uint32_t excl = 0;
+  if (tile > 0) {
+    bool gave_up = false;
+    excl = onesweep_lookback(status, tile, tid, &gave_up);
+    if (gave_up) report_error(err, kErrLookbackTimeout);
+    st_relaxed_u32(my_status, kStPrefix | ((excl + tile_cnt) & kStValueMask));
+  }
+  __syncthreads();
+  {
+    uint32_t before = 0;
+    for (unsigned j = 0; j < warp; ++j) before += s_warp_sum[j];
+    const uint32_t local_start = before + incl - tile_cnt;
+    s_local_start[tid] = local_start;
+    s_adj[tid] = digit_start[pass * kRadix + tid] + excl - local_start;
+  }
+
+  // Stable rank within the warp: per item, the lanes holding the same digit
+  // are found with eight ballots (one per digit bit); the lowest such lane
+  // advances the warp's counter for that digit and every lane adds the count
+  // of same-digit lanes below it.
   const unsigned lt = lanemask_lt();
 #pragma unroll
   for (int i = 0; i < IPT; ++i) {
-    const uint32_t idx = warp_base + i * kWarp + lane;
-    const bool valid = idx < n;
-    const uint32_t d = valid ? (uint32_t(radix_key_rt<U>(key[i], kind, desc) >> shift) & (kRadix - 1)) : 0x100u;
-    const unsigned grp = __match_any_sync(0xffffffffu, d);
+    const bool valid = !(dr[i] & 0x80000000u);
+    const uint32_t d = dr[i] & 0xffu;
+    unsigned grp = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < kRadixBits; ++b) {
+      const bool bit = (d >> b) & 1u;
+      const unsigned v = __ballot_sync(0xffffffffu, bit);
+      grp &= bit ? v : ~v;
+    }
     const int leader = __ffs(grp) - 1;
     uint32_t old = 0;
     if (valid && int(lane) == leader) {
       old = wcnt[warp * kRadix + d];
       wcnt[warp * kRadix + d] = old + __popc(grp);
     }
-    old = __shfl_sync(0xffffffffu, old, leader);
-    dr[i] = valid ? (d | ((old + __popc(grp & lt)) << 8)) : 0x80000000u;
+    old = __shfl_sync(0xffffffffu, old, valid ? leader : int(lane));
+    if (valid) dr[i] = d | ((old + __popc(grp & lt)) << 8);
     __syncwarp();
   }
   __syncthreads();
-
-  // Per digit (thread d): exclusive prefix across warps, tile count, publish.
-  uint32_t tile_cnt = 0;
-  if (tid < kRadix) {
+  // Exclusive prefix of each digit's count across warps.
+  {
     uint32_t run = 0;
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) {
@@ -266,81 +383,35 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
       wcnt[w * kRadix + tid] = run;
       run += c;
     }
-    tile_cnt = run;
-    uint32_t *st = status + size_t(tile) * kRadix + tid;
-    if (tile == 0) st_release_u32(st, kStPrefix | tile_cnt);
-    else st_release_u32(st, kStAggregate | tile_cnt);
-  }
-  // Tile-local exclusive scan of the digit counts (threads 0..255).
-  uint32_t incl = tile_cnt;
-#pragma unroll
-  for (int o = 1; o < kWarp; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (int(lane) >= o) incl += t;
-  }
-  if (tid < kRadix && lane == kWarp - 1) s_warp_sum[warp] = incl;
-  __syncthreads();
-  if (tid < kRadix) {
-    uint32_t before = 0;
-    for (unsigned j = 0; j < warp; ++j) before += s_warp_sum[j];
-    const uint32_t local_start = before + incl - tile_cnt;
-    s_local_start[tid] = local_start;
-    // Decoupled look-back for digit tid.
-    uint32_t excl = 0;
-    if (tile > 0) {
-      int64_t t = int64_t(tile) - 1;
-      bool gave_up = false;
-      while (t >= 0) {
-        const uint32_t *p = status + size_t(t) * kRadix + tid;
-        uint32_t w = ld_acquire_u32(p);
-        uint32_t spins = 0;
-        while ((w >> kStFlagShift) == 0) {
-          if (++spins > kSpinLimit) {
-            gave_up = true;
-            break;
-          }
-          __nanosleep(spins < 32 ? 20 : 200);
-          w = ld_acquire_u32(p);
-        }
-        if (gave_up) break;
-        excl += w & kStValueMask;
-        if ((w & kStPrefix) == kStPrefix && (w >> kStFlagShift) == 2u) break;
-        --t;
-      }
-      if (gave_up) report_error(err, kErrLookbackTimeout);
-      st_release_u32(status + size_t(tile) * kRadix + tid, kStPrefix | ((excl + tile_cnt) & kStValueMask));
-    }
-    s_adj[tid] = digit_start[pass * kRadix + tid] + excl - local_start;
   }
   __syncthreads();
 
-  // Stage keys and values in digit order.
+  // Digit-order position of every item: record its load index and digit.
 #pragma unroll
   for (int i = 0; i < IPT; ++i) {
     if (!(dr[i] & 0x80000000u)) {
       const uint32_t d = dr[i] & 0xffu;
       const uint32_t pos = s_local_start[d] + wcnt[warp * kRadix + d] + (dr[i] >> 8);
-      s_keys[pos] = key[i];
-      if (VB) s_vals[pos] = val[i];
+      s_perm[pos] = uint16_t(warp_first + i * kWarp + lane);
+      s_digit[pos] = uint8_t(d);
     }
   }
   __syncthreads();
 
-  // Write out: consecutive threads take consecutive staged elements, so each
-  // digit's run is written to consecutive addresses.
+  // Write out: consecutive threads take consecutive digit-order positions, so
+  // each digit's run is written to consecutive addresses.
   const uint32_t tile_valid = (n - tile_base) < uint32_t(TILE) ? (n - tile_base) : uint32_t(TILE);
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
     const uint32_t idx = k * kSortThreads + tid;
     if (idx < tile_valid) {
-      const U kv = s_keys[idx];
-      const uint32_t d = uint32_t(radix_key_rt<U>(kv, kind, desc) >> shift) & (kRadix - 1);
-      const uint32_t dst = s_adj[d] + idx;
+      const uint32_t li = s_perm[idx];
+      const uint32_t dst = s_adj[s_digit[idx]] + idx;
       // Always in range unless a look-back wait gave up (then the error word
       // is set and the output is garbage, but no write leaves the buffer).
       if (dst < n) {
-        dst_k[dst] = kv;
-        if (VB) dst_v[dst] = s_vals[idx];
+        dst_k[dst] = s_keys[li];
+        if (VB) dst_v[dst] = s_vals[li];
       }
     }
   }
@@ -428,8 +499,6 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
                         void *temp, size_t *temp_bytes) {
   typedef typename value_type_of<VB>::type VT;
   constexpr int PASSES = int(sizeof(U));
-  constexpr int IPT = items_per_thread<U>::value;
-  constexpr int TILE = kSortThreads * IPT;
   BCX_CHECK(n < kMaxSortN, BCX_INVALID_VALUE, "radix sort: n must be below 2^30 (got %zu)", n);
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
@@ -472,7 +541,7 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
     rc = launch_status("radix_prep");
     if (rc) return rc;
   }
-  const size_t smem = size_t(kSortWarps) * kRadix * 4 + size_t(TILE) * sizeof(U) + (VB ? size_t(TILE) * sizeof(VT) : 0);
+  const size_t smem = OnesweepSmem<U, VB>::kBytes;
   static bool attr_set = false;
   if (!attr_set) {
     BCX_CUDA(cudaFuncSetAttribute(radix_onesweep_kernel<U, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
