@@ -65,6 +65,12 @@ SIGNATURES = {
     "bcx_transform_binary": (_i, [_vp, _i, _i, _vp, _vp, _vp, _sz]),
     "bcx_transform_saxpy": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _sz]),
     "bcx_reduce_by_key": (_i, [_vp, _i, _i, _i, _vp, _vp, _sz, _vp, _vp, _vp, _i, _vp, _szp]),
+    "bcx_jit_get_kernel": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(_vp)]),
+    "bcx_jit_launch": (_i, [_vp, C.c_uint, C.c_uint, _sz, _vp, C.POINTER(_vp)]),
+    "bcx_jit_build_log": (_i, [C.c_char_p, _sz, _szp]),
+    "bcx_jit_cache_stats": (_i, [C.POINTER(C.c_uint64)] * 5),
+    "bcx_jit_cache_configure": (_i, [_sz, _i]),
+    "bcx_device_sm_count": (_i, [C.POINTER(_i)]),
     "bcx_profile_enable": (_i, [_i]),
     "bcx_profile_reset": (_i, []),
     "bcx_profile_read": (_i, [C.c_char_p, _sz, C.POINTER(C.c_uint64), C.POINTER(C.c_double), _sz, _szp]),

@@ -194,6 +194,31 @@ bcx_status bcx_reduce_by_key(bcx_stream stream, bcx_dtype key_type,
                              uint64_t *num_runs_dev, int compensated,
                              void *temp, size_t *temp_bytes);
 
+/* ---- run-time compiled kernels ------------------------------------------
+ * Replaces clBuildProgram + program_cache (utility/program_cache.hpp:52-168,
+ * program.hpp:638-692) and the offline binary cache (program.hpp:656-690):
+ * `source` is CUDA C++ generated by the drop-in headers for user functions,
+ * lambda expressions and iterator expressions (detail/meta_kernel.hpp).  It
+ * is compiled once with NVRTC for the current device's architecture and
+ * cached (LRU, 256 modules by default; cubins also kept in $BCX_CACHE_DIR when
+ * set).  A failed build returns BCX_BUILD_PROGRAM_FAILURE; the NVRTC log is
+ * then available from bcx_jit_build_log.  Kernel handles stay valid until
+ * their module is evicted: fetch the handle right before each launch. */
+typedef void *bcx_jit_kernel;
+bcx_status bcx_jit_get_kernel(const char *source, const char *kernel_name, const char *options,
+                              bcx_jit_kernel *kernel);
+/* Launch `kernel` (args as for cudaLaunchKernel) on `stream`. */
+bcx_status bcx_jit_launch(bcx_jit_kernel kernel, unsigned grid, unsigned block, size_t shared_bytes,
+                          bcx_stream stream, void **args);
+bcx_status bcx_jit_build_log(char *buf, size_t len, size_t *needed);
+bcx_status bcx_jit_cache_stats(uint64_t *hits, uint64_t *misses, uint64_t *compiles,
+                               uint64_t *disk_hits, uint64_t *entries);
+/* capacity 0 keeps the current capacity; clear != 0 unloads every module. */
+bcx_status bcx_jit_cache_configure(size_t capacity, int clear);
+/* Streaming multiprocessors of the current device (grid sizing of generated
+ * kernels). */
+bcx_status bcx_device_sm_count(int *sm_count);
+
 /* ---- profiling (command_queue::enable_profiling / event::duration,
  *      command_queue.hpp:82, event.hpp:269) --------------------------------
  * When enabled, every kernel this library launches is bracketed by CUDA

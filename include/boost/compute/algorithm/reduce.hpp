@@ -13,6 +13,7 @@
 
 #include <boost/compute/detail/device_range.hpp>
 #include <boost/compute/functional.hpp>
+#include <boost/compute/iterator/transform_iterator.hpp>
 
 namespace boost {
 namespace compute {
@@ -22,11 +23,11 @@ template <class F>
 using not_queue = typename std::enable_if<!std::is_same<typename std::decay<F>::type, command_queue>::value>::type;
 }  // namespace detail
 
-// device result
-template <class InputIterator, class T, class BinaryFunction, class = detail::not_queue<BinaryFunction> >
+// device result, built-in functor
+template <class InputIterator, class T, class BinaryFunction, class = detail::not_queue<BinaryFunction>,
+          class = typename std::enable_if<detail::is_builtin_binary<BinaryFunction>::value>::type>
 inline void reduce(InputIterator first, InputIterator last, buffer_iterator<T> result, BinaryFunction,
                    command_queue &queue = system::default_queue()) {
-  static_assert(detail::is_builtin_binary<BinaryFunction>::value, "reduce: built-in functors only");
   if (first == last) return;
   detail::device_range<InputIterator> in(first, last, queue);
   const int comp = std::is_floating_point<T>::value && BinaryFunction::bcx_op == BCX_PLUS;
@@ -50,7 +51,29 @@ inline void reduce(InputIterator first, InputIterator last, OutputIterator resul
   ::boost::compute::reduce(first, last, result, plus<T>(), queue);
 }
 
-template <class InputIterator, class T, class BinaryFunction, class = detail::not_queue<BinaryFunction> >
+// device result, lambda or BOOST_COMPUTE_FUNCTION (associative)
+template <class InputIterator, class T, class F, class = typename std::enable_if<detail::is_jit_functor<F>::value>::type>
+inline void reduce(InputIterator first, InputIterator last, buffer_iterator<T> result, F f,
+                   command_queue &queue = system::default_queue()) {
+  if (first == last) return;
+  detail::device_range<InputIterator> in(first, last, queue);
+  detail::jit_reduce(f.defs(), f.print(), detail::cuda_type_name<T>::get(), sizeof(T), in.ptr, in.n, nullptr,
+                     result.get_ptr(), queue);
+}
+
+template <class InputIterator, class T, class F,
+          class = typename std::enable_if<detail::is_jit_functor<F>::value>::type>
+inline T accumulate(InputIterator first, InputIterator last, T init, F f, command_queue &queue = system::default_queue()) {
+  if (first == last) return init;
+  detail::device_range<InputIterator> in(first, last, queue);
+  vector<T> tmp(1, queue.get_context());
+  detail::jit_reduce(f.defs(), f.print(), detail::cuda_type_name<T>::get(), sizeof(T), in.ptr, in.n, &init,
+                     tmp.data(), queue);
+  return tmp.begin().read(queue);
+}
+
+template <class InputIterator, class T, class BinaryFunction, class = detail::not_queue<BinaryFunction>,
+          class = typename std::enable_if<detail::is_builtin_binary<BinaryFunction>::value>::type>
 inline T accumulate(InputIterator first, InputIterator last, T init, BinaryFunction,
                     command_queue &queue = system::default_queue()) {
   typedef typename std::iterator_traits<InputIterator>::value_type IT;

@@ -11,16 +11,26 @@
 
 #include <boost/compute/detail/device_range.hpp>
 #include <boost/compute/functional.hpp>
+#include <boost/compute/iterator/transform_iterator.hpp>
 
 namespace boost {
 namespace compute {
 namespace detail {
 
+template <class InputIterator, class T, class F>
+inline typename std::enable_if<is_jit_functor<F>::value, buffer_iterator<T> >::type
+scan(InputIterator first, InputIterator last, buffer_iterator<T> result, bool exclusive, T init, F f,
+     command_queue &queue) {
+  device_range<InputIterator> in(first, last, queue);
+  jit_scan(f.defs(), f.print(), cuda_type_name<T>::get(), sizeof(T), in.ptr, result.get_ptr(), in.n, exclusive,
+           &init, queue);
+  return result + std::ptrdiff_t(in.n);
+}
+
 template <class InputIterator, class T, class BinaryOperator>
-inline buffer_iterator<T> scan(InputIterator first, InputIterator last, buffer_iterator<T> result, bool exclusive,
-                               T init, BinaryOperator, command_queue &queue) {
-  static_assert(is_builtin_binary<BinaryOperator>::value,
-                "scan: only the built-in functors are provided on this path");
+inline typename std::enable_if<is_builtin_binary<BinaryOperator>::value, buffer_iterator<T> >::type
+scan(InputIterator first, InputIterator last, buffer_iterator<T> result, bool exclusive, T init, BinaryOperator,
+     command_queue &queue) {
   device_range<InputIterator> in(first, last, queue);
   const int comp = std::is_floating_point<T>::value && BinaryOperator::bcx_op == BCX_PLUS;
   detail::check(bcx_scan(queue.get(), bcx_dtype(bcx_dtype_of<T>()), bcx_op(BinaryOperator::bcx_op),

@@ -12,6 +12,7 @@
 
 #include <boost/compute/detail/device_range.hpp>
 #include <boost/compute/functional.hpp>
+#include <boost/compute/iterator/transform_iterator.hpp>
 
 namespace boost {
 namespace compute {
@@ -35,6 +36,34 @@ transform(InputIterator1 first1, InputIterator1 last1, InputIterator2 first2, bu
   detail::device_range<InputIterator2> b(first2, first2 + std::ptrdiff_t(a.n), queue);
   detail::check(bcx_transform_binary(queue.get(), bcx_dtype(detail::bcx_dtype_of<T>()),
                                      bcx_op(BinaryFunction::bcx_op), a.ptr, b.ptr, result.get_ptr(), a.n));
+  queue.finish();
+  return result + std::ptrdiff_t(a.n);
+}
+
+// Lambda expressions and BOOST_COMPUTE_FUNCTIONs: one generated kernel.
+template <class InputIterator, class T, class F>
+inline typename std::enable_if<detail::is_jit_functor<F>::value, buffer_iterator<T> >::type
+transform(InputIterator first, InputIterator last, buffer_iterator<T> result, F f,
+          command_queue &queue = system::default_queue()) {
+  typedef typename std::iterator_traits<InputIterator>::value_type A;
+  detail::device_range<InputIterator> in(first, last, queue);
+  detail::jit_transform(f.defs(), f.print(), detail::cuda_type_name<A>::get(), "", detail::cuda_type_name<T>::get(),
+                        sizeof(A), 0, sizeof(T), in.ptr, nullptr, result.get_ptr(), in.n, queue);
+  if (!std::is_same<InputIterator, buffer_iterator<A> >::value) queue.finish();
+  return result + std::ptrdiff_t(in.n);
+}
+
+template <class InputIterator1, class InputIterator2, class T, class F>
+inline typename std::enable_if<detail::is_jit_functor<F>::value, buffer_iterator<T> >::type
+transform(InputIterator1 first1, InputIterator1 last1, InputIterator2 first2, buffer_iterator<T> result, F f,
+          command_queue &queue = system::default_queue()) {
+  typedef typename std::iterator_traits<InputIterator1>::value_type A;
+  typedef typename std::iterator_traits<InputIterator2>::value_type B;
+  detail::device_range<InputIterator1> a(first1, last1, queue);
+  detail::device_range<InputIterator2> b(first2, first2 + std::ptrdiff_t(a.n), queue);
+  detail::jit_transform(f.defs(), f.print(), detail::cuda_type_name<A>::get(), detail::cuda_type_name<B>::get(),
+                        detail::cuda_type_name<T>::get(), sizeof(A), sizeof(B), sizeof(T), a.ptr, b.ptr,
+                        result.get_ptr(), a.n, queue);
   queue.finish();
   return result + std::ptrdiff_t(a.n);
 }

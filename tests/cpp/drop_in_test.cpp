@@ -4,6 +4,7 @@
 // suite (file:line given); the program prints one line per failure and exits
 // non-zero if any check failed.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <numeric>
@@ -170,6 +171,78 @@ static void reduce_by_key_cases(compute::command_queue &q) {
   CHECK((std::vector<int>(hv.begin(), hv.begin() + 4) == std::vector<int>{1, 1, 10, 1}));
 }
 
+static void jit_cases(compute::command_queue &q) {
+  using compute::_1;
+  using compute::_2;
+  // perf/perf_saxpy.cpp:50-56: alpha * _1 + _2 (one rounding, like fmaf)
+  const size_t n = (1 << 20) + 3;
+  std::vector<float> hx(n), hy(n);
+  std::mt19937 gen(5);
+  std::uniform_real_distribution<float> u(-1.f, 1.f);
+  for (size_t i = 0; i < n; ++i) { hx[i] = u(gen); hy[i] = u(gen); }
+  compute::vector<float> x(hx.begin(), hx.end(), q), y(hy.begin(), hy.end(), q), r(n, q.get_context());
+  const float alpha = 2.5f;
+  compute::transform(x.begin(), x.end(), y.begin(), r.begin(), alpha * _1 + _2, q);
+  std::vector<float> hr = to_host(r, q);
+  bool exact = true;
+  for (size_t i = 0; i < n; ++i) exact = exact && hr[i] == std::fma(alpha, hx[i], hy[i]);
+  CHECK(exact);
+  // test/test_transform.cpp:61-73 (clamp)
+  float cd[] = {10.f, 20.f, 30.f, 40.f, 50.f};
+  compute::vector<float> cv(cd, cd + 5, q);
+  compute::transform(cv.begin(), cv.end(), cv.begin(), clamp(_1, 15.f, 45.f), q);
+  CHECK((to_host(cv, q) == std::vector<float>{15.f, 20.f, 30.f, 40.f, 45.f}));
+  // test/test_transform.cpp:101-118 (pown)
+  float pd[] = {1.f, 2.f, 3.f, 4.f};
+  compute::vector<float> pv(pd, pd + 4, q), po(4, q.get_context());
+  compute::transform(pv.begin(), pv.end(), po.begin(), pown(_1, 4), q);
+  CHECK((to_host(po, q) == std::vector<float>{1.f, 16.f, 81.f, 256.f}));
+  // test/test_transform.cpp:120-141 (BOOST_COMPUTE_FUNCTION)
+  float fd[] = {9.f, 7.f, 5.f, 3.f};
+  compute::vector<float> fv(fd, fd + 4, q), fo(4, q.get_context());
+  BOOST_COMPUTE_FUNCTION(float, pow3add4, (float x), { return pow(x, 3.0f) + 4.0f; });
+  compute::transform(fv.begin(), fv.end(), fo.begin(), pow3add4, q);
+  std::vector<float> hfo = to_host(fo, q);
+  CHECK(std::fabs(hfo[0] - 733.f) < 1e-3f && std::fabs(hfo[3] - 31.f) < 1e-4f);
+  // test/test_closure.cpp:32-47 (BOOST_COMPUTE_CLOSURE)
+  int two = 2;
+  BOOST_COMPUTE_CLOSURE(int, add_two, (int x), (two), { return x + two; });
+  int id[] = {1, 2, 3, 4};
+  compute::vector<int> iv(id, id + 4, q);
+  compute::transform(iv.begin(), iv.end(), iv.begin(), add_two, q);
+  CHECK((to_host(iv, q) == std::vector<int>{3, 4, 5, 6}));
+  // test/test_scan.cpp:438-488 (custom function scans)
+  BOOST_COMPUTE_FUNCTION(int, multi, (int x, int y), { return x * y * 2; });
+  int sd[] = {1, 2, 1, 2, 3};
+  compute::vector<int> sv(sd, sd + 5, q), so(5, q.get_context());
+  compute::inclusive_scan(sv.begin(), sv.end(), so.begin(), multi, q);
+  CHECK((to_host(so, q) == std::vector<int>{1, 4, 8, 32, 192}));
+  compute::exclusive_scan(sv.begin(), sv.end(), so.begin(), 1, multi, q);
+  CHECK((to_host(so, q) == std::vector<int>{1, 2, 8, 16, 64}));
+  compute::exclusive_scan(sv.begin(), sv.end(), sv.begin(), 1, multi, q);  // in place
+  CHECK((to_host(sv, q) == std::vector<int>{1, 2, 8, 16, 64}));
+  // test/test_scan.cpp:258-285 (scan of a transform_iterator)
+  float td[] = {1.f, 2.f, 3.f, 4.f, 5.f};
+  compute::vector<float> tv(td, td + 5, q), to(5, q.get_context());
+  compute::inclusive_scan(compute::make_transform_iterator(tv.begin(), pown(_1, 2)),
+                          compute::make_transform_iterator(tv.end(), pown(_1, 2)), to.begin(), q);
+  CHECK((to_host(to, q) == std::vector<float>{1.f, 5.f, 14.f, 30.f, 55.f}));
+  // a user functor in reduce/accumulate (associative)
+  BOOST_COMPUTE_FUNCTION(int, add3, (int a, int b), { return a + b; });
+  compute::vector<int> big(100003, q.get_context());
+  compute::iota(big.begin(), big.end(), 0, q);
+  CHECK(compute::accumulate(big.begin(), big.end(), 5, add3, q) == int(5 + (100003LL * 100002 / 2) % (1LL << 32)));
+  // a build failure surfaces as program_build_failure with the log
+  BOOST_COMPUTE_FUNCTION(int, broken, (int x), { return x +; });
+  bool threw = false;
+  try {
+    compute::transform(iv.begin(), iv.end(), iv.begin(), broken, q);
+  } catch (const compute::program_build_failure &e) {
+    threw = !e.build_log().empty();
+  }
+  CHECK(threw);
+}
+
 static void error_cases(compute::command_queue &q) {
   // bcx errors surface as opencl_error with the OpenCL status code
   bool thrown = false;
@@ -190,6 +263,7 @@ int main() {
   reduce_cases(q);
   transform_cases(q);
   reduce_by_key_cases(q);
+  jit_cases(q);
   error_cases(q);
   q.check_device_errors();
   std::printf("%s (%d failures)\n", g_failures ? "FAILED" : "OK", g_failures);
