@@ -59,6 +59,7 @@ SIGNATURES = {
     "bcx_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _i, _vp, _szp]),
     "bcx_sort_pairs_host": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _i]),
     "bcx_scan": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _sz, _i, _vp, _szp]),
+    "bcx_scan_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _sz, _i]),
     "bcx_reduce": (_i, [_vp, _i, _i, _vp, _sz, _vp, _i, _vp, _szp]),
     "bcx_accumulate": (_i, [_vp, _i, _i, _vp, _sz, _vp, _vp, _i, _vp, _szp]),
     "bcx_transform_unary": (_i, [_vp, _i, _i, _vp, _vp, _sz]),

@@ -24,6 +24,9 @@
 
 #include <string.h>
 
+#include <map>
+#include <mutex>
+
 #include "bcx.h"
 #include "bcx_common.cuh"
 #include "bcx_internal.h"
@@ -473,6 +476,170 @@ extern "C" bcx_status bcx_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int
     case BCX_ULONG: rc = dispatch_int<unsigned long long>(s, op, exclusive, init_p, in, out, n, temp, temp_bytes); break;
     case BCX_FLOAT: rc = dispatch_float<float>(s, op, exclusive, init_p, in, out, n, compensated, temp, temp_bytes); break;
     case BCX_DOUBLE: rc = dispatch_float<double>(s, op, exclusive, init_p, in, out, n, compensated, temp, temp_bytes); break;
+  }
+  if (rc == BCX_UNSUPPORTED) set_error("scan: functor %d not provided for dtype %d", int(op), int(type));
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Scan that allocates nothing.
+//
+// Some callers cannot allocate device memory at the point where they need a
+// scan: a host application that owns every device allocation through its own
+// pool and forbids libraries from calling cudaMalloc, or a latency-critical
+// path where cudaMalloc/cudaFree (which may synchronize the device) is not
+// acceptable.  bcx_scan_noalloc serves them: its look-back scratch (the tile
+// ticket and the per-tile status words) lives in one fixed array compiled
+// into this library, so the call needs only the caller's input and output.
+//
+// The array is kNoAllocScratchBytes (4 MiB) on every GPU that loads the
+// library and stays allocated until the process exits.  All calls share it:
+// each call clears the part it uses on its own stream before the scan kernel
+// runs, so back-to-back calls are fine, but calls whose work overlaps on the
+// GPU (different streams, or different host threads) race on the array and
+// must be serialized by the caller.
+namespace bcx {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[kNoAllocScratchBytes];
+
+// Device address of the scratch array on the current device.  In host code
+// the array's name only stands in for the symbol, so the address is looked up
+// once per device (with that device current) and cached.
+static std::mutex g_noalloc_mu;
+static std::map<int, void *> g_noalloc_ptr;
+
+bcx_status noalloc_scratch(void **out) {
+  int dev = 0;
+  BCX_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  auto it = g_noalloc_ptr.find(dev);
+  if (it != g_noalloc_ptr.end()) {
+    *out = it->second;
+    return BCX_SUCCESS;
+  }
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(scan scratch)");
+  g_noalloc_ptr[dev] = p;
+  *out = p;
+  return BCX_SUCCESS;
+}
+
+template <class T, class P>
+bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, const void *in, void *out,
+                              size_t n) {
+  typedef typename P::Carry Carry;
+  typedef TileStatus<Carry> Status;
+  constexpr int N = 16 / sizeof(T);
+  constexpr int V = scan_vectors_per_thread<T>::value;
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
+  void *scratch = nullptr;
+  rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  const uintptr_t ain = reinterpret_cast<uintptr_t>(in), aout = reinterpret_cast<uintptr_t>(out);
+  const bool elem_aligned = (ain % sizeof(T) == 0) && (aout % sizeof(T) == 0);
+  const bool vec_ok = elem_aligned && ((ain & 15u) == (aout & 15u));
+  const size_t head_pad = vec_ok ? (ain & 15u) / sizeof(T) : 0;
+  const size_t tile_elems = size_t(kScanThreads) * V * N;
+  const size_t tiles = div_up(n + head_pad, tile_elems);
+  const Carry init_carry = P::host_carry(init);
+  const T *pin = static_cast<const T *>(in);
+  T *pout = static_cast<T *>(out);
+  if (tiles <= 1) {
+    Status st{};
+    KernelScope ks("scan_single", s);
+    scan_tile_kernel<T, P, V, true, Status><<<1, kScanThreads, 0, s>>>(
+        pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, nullptr, ds->err_word);
+    return launch_status("scan_single");
+  }
+  const size_t need = 256 + Status::bytes(tiles);
+  if (need > kNoAllocScratchBytes) {
+    // Largest n whose tile status still fits in the array.
+    size_t lo = 0, hi = tiles;
+    while (lo + 1 < hi) {
+      const size_t mid = (lo + hi) / 2;
+      if (256 + Status::bytes(mid) <= kNoAllocScratchBytes) lo = mid;
+      else hi = mid;
+    }
+    set_error("bcx_scan_noalloc: n = %zu needs %zu bytes of scratch, more than its fixed %zu bytes; "
+              "at most %zu elements of this type/functor per call (use bcx_scan for more)",
+              n, need, kNoAllocScratchBytes, lo * tile_elems - head_pad);
+    return BCX_INVALID_BUFFER_SIZE;
+  }
+  char *base = static_cast<char *>(scratch);
+  uint32_t *counter = reinterpret_cast<uint32_t *>(base);
+  Status st;
+  st.bind(base + 256, tiles);
+  // The array keeps the previous call's tickets and flags: clear them.
+  BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
+  KernelScope ks("scan_lookback", s);
+  scan_tile_kernel<T, P, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
+      pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);
+  return launch_status("scan_lookback");
+}
+
+template <class T>
+bcx_status noalloc_int(cudaStream_t s, int op, int ex, const void *init, const void *in, void *out,
+                       size_t n) {
+  switch (op) {
+    case BCX_PLUS: return run_scan_noalloc_t<T, ScanPlain<T, op_plus>>(s, ex, init, in, out, n);
+    case BCX_MULTIPLIES: return run_scan_noalloc_t<T, ScanPlain<T, op_multiplies>>(s, ex, init, in, out, n);
+    case BCX_MIN: return run_scan_noalloc_t<T, ScanPlain<T, op_min>>(s, ex, init, in, out, n);
+    case BCX_MAX: return run_scan_noalloc_t<T, ScanPlain<T, op_max>>(s, ex, init, in, out, n);
+    case BCX_BIT_AND: return run_scan_noalloc_t<T, ScanPlain<T, op_bit_and>>(s, ex, init, in, out, n);
+    case BCX_BIT_OR: return run_scan_noalloc_t<T, ScanPlain<T, op_bit_or>>(s, ex, init, in, out, n);
+    case BCX_BIT_XOR: return run_scan_noalloc_t<T, ScanPlain<T, op_bit_xor>>(s, ex, init, in, out, n);
+  }
+  return BCX_UNSUPPORTED;
+}
+
+template <class T>
+bcx_status noalloc_float(cudaStream_t s, int op, int ex, const void *init, const void *in, void *out,
+                         size_t n, int comp) {
+  switch (op) {
+    case BCX_PLUS:
+      if (comp) {
+        if (sizeof(T) == 4) return run_scan_noalloc_t<float, ScanCompF32>(s, ex, init, in, out, n);
+        return run_scan_noalloc_t<double, ScanCompF64>(s, ex, init, in, out, n);
+      }
+      return run_scan_noalloc_t<T, ScanPlain<T, op_plus>>(s, ex, init, in, out, n);
+    case BCX_MULTIPLIES: return run_scan_noalloc_t<T, ScanPlain<T, op_multiplies>>(s, ex, init, in, out, n);
+    case BCX_MIN: return run_scan_noalloc_t<T, ScanPlain<T, op_min>>(s, ex, init, in, out, n);
+    case BCX_MAX: return run_scan_noalloc_t<T, ScanPlain<T, op_max>>(s, ex, init, in, out, n);
+  }
+  return BCX_UNSUPPORTED;
+}
+
+}  // namespace
+}  // namespace bcx
+
+extern "C" bcx_status bcx_scan_noalloc(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive,
+                                       const void *init, const void *in, void *out, size_t n,
+                                       int compensated) {
+  using namespace bcx;
+  clear_error();
+  BCX_CHECK(dtype_valid(type), BCX_INVALID_VALUE, "invalid dtype %d", int(type));
+  if (n == 0) return BCX_SUCCESS;
+  BCX_CHECK(in != nullptr && out != nullptr, BCX_INVALID_VALUE, "NULL input or output");
+  unsigned char zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const void *init_p = (exclusive && init) ? init : zero;
+  cudaStream_t s = (cudaStream_t)stream;
+  bcx_status rc = BCX_UNSUPPORTED;
+  switch (type) {
+    case BCX_CHAR: rc = noalloc_int<int8_t>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_UCHAR: rc = noalloc_int<uint8_t>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_SHORT: rc = noalloc_int<int16_t>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_USHORT: rc = noalloc_int<uint16_t>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_INT: rc = noalloc_int<int32_t>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_UINT: rc = noalloc_int<uint32_t>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_LONG: rc = noalloc_int<long long>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_ULONG: rc = noalloc_int<unsigned long long>(s, op, exclusive, init_p, in, out, n); break;
+    case BCX_FLOAT: rc = noalloc_float<float>(s, op, exclusive, init_p, in, out, n, compensated); break;
+    case BCX_DOUBLE: rc = noalloc_float<double>(s, op, exclusive, init_p, in, out, n, compensated); break;
   }
   if (rc == BCX_UNSUPPORTED) set_error("scan: functor %d not provided for dtype %d", int(op), int(type));
   return rc;

@@ -148,6 +148,24 @@ bcx_status bcx_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive,
                     const void *init, const void *in, void *out, size_t n,
                     int compensated, void *temp, size_t *temp_bytes);
 
+/* Scan that allocates nothing (no counterpart in the reference: Boost.Compute
+ * always allocates its temporaries per call).  For callers that cannot call
+ * cudaMalloc when they scan -- a host application whose own pool owns every
+ * device allocation, or a latency-critical path where an allocation that may
+ * synchronize the device is not acceptable.  Same types, functors, init and
+ * in-place rules as bcx_scan; the look-back scratch is one fixed 4 MiB array
+ * inside libbcx that every GPU loading the library keeps until exit.  Limit:
+ * at most 2^30 elements per call for 1-4 byte types, about 2^27-2^28 for
+ * 8-byte types (the exact bound depends on the carry type); larger n is
+ * rejected with BCX_INVALID_BUFFER_SIZE and a message giving the bound.  The
+ * first call on each device looks up the array's device address; make that
+ * first call before any stream capture.  Every call reuses the array (each
+ * clears what it needs on its own stream first), so calls whose work
+ * overlaps on the GPU race and must be serialized by the caller. */
+bcx_status bcx_scan_noalloc(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive,
+                            const void *init, const void *in, void *out, size_t n,
+                            int compensated);
+
 /* ---- reduce / accumulate -------------------------------------------------
  * reduce(first, last, result, op) into ONE device value at out_dev
  * (reduce.hpp:205-305, detail/reduce_on_gpu.hpp:169-280).  n == 0 writes
