@@ -57,11 +57,31 @@ constexpr size_t kMaxSortN = size_t(1) << 30;
 
 enum KeyKind : int { kKeyUnsigned = 0, kKeySigned = 1, kKeyFloat = 2 };
 
+
+// The radix() transform as four masks chosen on the host, so kernels apply it
+// without branches: key = ((x ^ a) + b) ^ ((f & -(x >> sign)) | c).
+//   ascending unsigned a=0  b=0 f=0  c=0        descending unsigned a=~0 b=0 f=0  c=0
+//   ascending signed   a=0  b=0 f=0  c=sign     descending signed   a=~0 b=1 f=0  c=sign
+//   ascending float    a=0  b=0 f=~0 c=sign     descending float    a=~0 b=1 f=~0 c=sign
+// (~x + 1 is -x; the float mask is taken from x, as the reference does.)
 template <class U>
-__device__ __forceinline__ U radix_key_rt(U x, int kind, int desc) {
-  if (kind == kKeyFloat) return desc ? radix_key<U, true, true, true>(x) : radix_key<U, true, true, false>(x);
-  if (kind == kKeySigned) return desc ? radix_key<U, false, true, true>(x) : radix_key<U, false, true, false>(x);
-  return desc ? radix_key<U, false, false, true>(x) : radix_key<U, false, false, false>(x);
+struct KeyXform {
+  U a, b, f, c;
+};
+template <class U>
+KeyXform<U> make_xform(int kind, int desc) {
+  const U sign = U(U(1) << (sizeof(U) * 8 - 1));
+  KeyXform<U> x;
+  x.a = desc ? U(~U(0)) : U(0);
+  x.b = (desc && kind != kKeyUnsigned) ? U(1) : U(0);
+  x.f = kind == kKeyFloat ? U(~U(0)) : U(0);
+  x.c = kind == kKeyUnsigned ? U(0) : sign;
+  return x;
+}
+template <class U>
+__device__ __forceinline__ U apply_xform(U x, const KeyXform<U> &t) {
+  constexpr int kSign = int(sizeof(U) * 8 - 1);
+  return U(U(U(x ^ t.a) + t.b) ^ U((t.f & U(U(0) - U(x >> kSign))) | t.c));
 }
 
 template <int VB> struct value_type_of;
@@ -105,7 +125,7 @@ __device__ __forceinline__ void hist_count(uint32_t (*sh)[kRadix], U k, bool val
 
 template <class U, int PASSES>
 __global__ void __launch_bounds__(kHistThreads)
-radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t nvec, int kind, int desc,
+radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t nvec, const KeyXform<U> xf,
                        uint32_t *__restrict__ hist) {
   constexpr int N = 16 / sizeof(U);
   __shared__ uint32_t sh[PASSES][kRadix];
@@ -119,11 +139,11 @@ radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t
     const size_t tail = head + nvec * N;
     for (size_t b = 0; b < head; b += kWarp) {
       const bool valid = b + lane < head;
-      hist_count<U, PASSES>(sh, valid ? radix_key_rt<U>(keys[b + lane], kind, desc) : U(0), valid, lane);
+      hist_count<U, PASSES>(sh, valid ? apply_xform<U>(keys[b + lane], xf) : U(0), valid, lane);
     }
     for (size_t b = tail; b < n; b += kWarp) {
       const bool valid = b + lane < n;
-      hist_count<U, PASSES>(sh, valid ? radix_key_rt<U>(keys[b + lane], kind, desc) : U(0), valid, lane);
+      hist_count<U, PASSES>(sh, valid ? apply_xform<U>(keys[b + lane], xf) : U(0), valid, lane);
     }
   }
   const vec16<U> *vk = reinterpret_cast<const vec16<U> *>(keys + head);
@@ -134,7 +154,7 @@ radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t
     if (valid) r = ld_stream16(vk + v);
 #pragma unroll
     for (int j = 0; j < N; ++j)
-      hist_count<U, PASSES>(sh, valid ? radix_key_rt<U>(r.v[j], kind, desc) : U(0), valid, lane);
+      hist_count<U, PASSES>(sh, valid ? apply_xform<U>(r.v[j], xf) : U(0), valid, lane);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) {
@@ -247,7 +267,7 @@ __global__ void __launch_bounds__(kSortThreads)
 radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
                       typename value_type_of<VB>::type *__restrict__ vals_main,
                       typename value_type_of<VB>::type *__restrict__ vals_alt, uint32_t n,
-                      int pass, int kind, int desc, const uint32_t *__restrict__ digit_start,
+                      int pass, const KeyXform<U> xf, const uint32_t *__restrict__ digit_start,
                       uint32_t *__restrict__ status, uint32_t *__restrict__ tile_counter,
                       const SortControl *__restrict__ ctrl, uint32_t *err) {
   typedef OnesweepSmem<U, VB> L;
@@ -289,7 +309,25 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
   // so (i, l) order is input order), stage in shared memory in that order,
   // and count digits.
   uint32_t dr[IPT];  // digit | rank-within-warp << 8 | invalid << 31
-  {
+  const bool full = tile_base + uint32_t(TILE) <= n;
+  if (full) {
+    U key[IPT];
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) key[i] = src_k[tile_base + warp_first + i * kWarp + lane];
+    if (VB) {
+      VT val[VB ? IPT : 1];
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) val[i] = src_v[tile_base + warp_first + i * kWarp + lane];
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) s_vals[warp_first + i * kWarp + lane] = val[i];
+    }
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      s_keys[warp_first + i * kWarp + lane] = key[i];
+      dr[i] = uint32_t(apply_xform<U>(key[i], xf) >> shift) & (kRadix - 1);
+      atomicAdd(&s_hist[dr[i]], 1u);
+    }
+  } else {
     U key[IPT];
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
@@ -311,7 +349,7 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
       const uint32_t li = warp_first + i * kWarp + lane;
       s_keys[li] = key[i];
       if (tile_base + li < n) {
-        dr[i] = uint32_t(radix_key_rt<U>(key[i], kind, desc) >> shift) & (kRadix - 1);
+        dr[i] = uint32_t(apply_xform<U>(key[i], xf) >> shift) & (kRadix - 1);
         atomicAdd(&s_hist[dr[i]], 1u);
       } else {
         dr[i] = 0x80000000u;
@@ -356,7 +394,7 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
   for (int i = 0; i < IPT; ++i) {
     const bool valid = !(dr[i] & 0x80000000u);
     const uint32_t d = dr[i] & 0xffu;
-    unsigned grp = __ballot_sync(0xffffffffu, valid);
+    unsigned grp = full ? 0xffffffffu : __ballot_sync(0xffffffffu, valid);
 #pragma unroll
     for (int b = 0; b < kRadixBits; ++b) {
       const bool bit = (d >> b) & 1u;
@@ -400,11 +438,11 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
 
   // Write out: consecutive threads take consecutive digit-order positions, so
   // each digit's run is written to consecutive addresses.
-  const uint32_t tile_valid = (n - tile_base) < uint32_t(TILE) ? (n - tile_base) : uint32_t(TILE);
+  const uint32_t tile_valid = full ? uint32_t(TILE) : (n - tile_base);
 #pragma unroll
   for (int k = 0; k < IPT; ++k) {
     const uint32_t idx = k * kSortThreads + tid;
-    if (idx < tile_valid) {
+    if (full || idx < tile_valid) {
       const uint32_t li = s_perm[idx];
       const uint32_t dst = s_adj[s_digit[idx]] + idx;
       // Always in range unless a look-back wait gave up (then the error word
@@ -519,6 +557,7 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
   uint32_t *counters = reinterpret_cast<uint32_t *>(base + L.counters);
   uint32_t *status = reinterpret_cast<uint32_t *>(base + L.status);
   BCX_CUDA(cudaMemsetAsync(base + L.zero_begin, 0, L.zero_bytes, s));
+  const KeyXform<U> xf = make_xform<U>(kind, desc);
   {
     KernelScope ks("radix_histogram", s);
     constexpr int N = 16 / sizeof(U);
@@ -530,8 +569,8 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
     size_t cap = size_t(ds->sm_count) * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    radix_histogram_kernel<U, PASSES><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, kind,
-                                                                                 desc, hist);
+    radix_histogram_kernel<U, PASSES><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, xf,
+                                                                                 hist);
     rc = launch_status("radix_histogram");
     if (rc) return rc;
   }
@@ -550,7 +589,7 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
   for (int p = 0; p < PASSES; ++p) {
     KernelScope ks("radix_onesweep", s);
     radix_onesweep_kernel<U, VB><<<L.tiles, kSortThreads, smem, s>>>(
-        k_main, k_alt, v_main, v_alt, uint32_t(n), p, kind, desc, hist, status + size_t(p) * L.tiles * kRadix,
+        k_main, k_alt, v_main, v_alt, uint32_t(n), p, xf, hist, status + size_t(p) * L.tiles * kRadix,
         counters + p, ctrl, ds->err_word);
     rc = launch_status("radix_onesweep");
     if (rc) return rc;
