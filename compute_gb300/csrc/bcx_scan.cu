@@ -191,8 +191,13 @@ struct TileStatus<Carry, false> {
 };
 
 // Warp 0 of a block: publish this tile's aggregate, look back for the
-// exclusive prefix, publish the inclusive prefix.  Returns the exclusive
-// prefix (valid in every lane of warp 0).
+// exclusive prefix, publish the inclusive prefix.  Lane l watches the
+// predecessors pred - l - 32*j for j < kLookbackDepth, all loaded at once, so
+// one L2 round trip covers 32 * kLookbackDepth predecessors: the walk back to
+// the nearest inclusive prefix stays short even when many tiles are in flight.
+// Returns the exclusive prefix (valid in every lane of warp 0).
+constexpr int kLookbackDepth = 4;
+
 template <class P, class Status>
 __device__ __forceinline__ typename P::Carry lookback(Status &st, size_t tile,
                                                       typename P::Carry agg, uint32_t *err) {
@@ -203,37 +208,46 @@ __device__ __forceinline__ typename P::Carry lookback(Status &st, size_t tile,
   long long pred = (long long)tile - 1;
   bool gave_up = false;
   while (true) {
-    long long t = pred - (long long)lane;
-    C v = P::carry_ident();
-    uint32_t f = kFlagPrefix;  // beyond tile 0: nothing to add
-    if (t >= 0) {
+    C v[kLookbackDepth];
+    uint32_t f[kLookbackDepth];
+#pragma unroll
+    for (int j = 0; j < kLookbackDepth; ++j) {
+      const long long t = pred - (long long)lane - (long long)kWarp * j;
+      v[j] = P::carry_ident();
+      f[j] = kFlagPrefix;  // beyond tile 0: nothing to add
+      if (t >= 0) f[j] = st.poll(size_t(t), &v[j]);
+    }
+    bool done = false;
+#pragma unroll
+    for (int j = 0; j < kLookbackDepth; ++j) {
+      if (done) break;
+      const long long t = pred - (long long)lane - (long long)kWarp * j;
       uint32_t spins = 0;
-      f = st.poll(size_t(t), &v);
-      while (f == kFlagInvalid) {
+      while (f[j] == kFlagInvalid) {
         if (++spins > kSpinLimit) {
           gave_up = true;
-          f = kFlagPrefix;
-          v = P::carry_ident();
+          f[j] = kFlagPrefix;
+          v[j] = P::carry_ident();
           break;
         }
-        if (spins > 16) __nanosleep(spins < 256 ? 32 : 256);
-        f = st.poll(size_t(t), &v);
+        if (spins > 32) __nanosleep(spins < 256 ? 32 : 256);
+        f[j] = st.poll(size_t(t), &v[j]);
       }
-    }
-    const unsigned pmask = __ballot_sync(0xffffffffu, f == kFlagPrefix);
-    const int first = pmask ? __ffs(pmask) - 1 : 31;
-    if (int(lane) > first) v = P::carry_ident();
-    // Lane 0 folds lanes 0..first: the window of predecessors nearest to this
-    // tile, ending at the nearest inclusive prefix.
+      const unsigned pmask = __ballot_sync(0xffffffffu, f[j] == kFlagPrefix);
+      const int first = pmask ? __ffs(pmask) - 1 : kWarp - 1;
+      C w = (int(lane) > first) ? P::carry_ident() : v[j];
+      // Lane 0 folds lanes 0..first: this window's predecessors up to the
+      // nearest inclusive prefix.
 #pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) {
-      C o = P::carry_shfl_down(v, d);
-      if (int(lane) + d < kWarp) v = P::carry_comb(v, o);
+      for (int d = 16; d >= 1; d >>= 1) {
+        C o = P::carry_shfl_down(w, d);
+        if (int(lane) + d < kWarp) w = P::carry_comb(w, o);
+      }
+      excl = P::carry_comb(P::carry_bcast(w), excl);
+      done = pmask != 0;
     }
-    const C window = P::carry_bcast(v);
-    excl = P::carry_comb(window, excl);
-    if (pmask) break;
-    pred -= 32;
+    if (done) break;
+    pred -= (long long)kWarp * kLookbackDepth;
   }
   if (__any_sync(0xffffffffu, gave_up) && lane == 0) report_error(err, kErrLookbackTimeout);
   if (lane == 0) st.publish(tile, kFlagPrefix, P::carry_comb(excl, agg));
@@ -368,162 +382,6 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   }
 }
 
-// Persistent, pipelined variant for 16-byte aligned input and output whose
-// byte length is a multiple of 16.  Each block keeps kPipeStages tiles in
-// flight: thread 0 takes tickets in increasing order and issues one bulk
-// asynchronous copy (TMA, 1-D) per tile into a shared-memory ring, so HBM keeps
-// streaming while the block waits on its look-back.  A block processes its
-// tickets in increasing order, so the smallest unfinished ticket's owner can
-// always proceed: no deadlock whatever the residency.
-constexpr int kPipeThreads = 256;
-constexpr int kPipeWarps = kPipeThreads / kWarp;
-constexpr int kPipeStages = 4;
-constexpr uint32_t kErrPipeTimeout = 2u;
-
-template <class T, class P, int V, class Status>
-__global__ void __launch_bounds__(kPipeThreads)
-scan_pipe_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, int exclusive,
-                 typename P::Carry init_carry, Status st, uint32_t *tile_counter, uint32_t tiles,
-                 uint32_t *err) {
-  typedef typename P::Acc Acc;
-  typedef typename P::Carry Carry;
-  constexpr int N = 16 / sizeof(T);
-  constexpr int TILE = kPipeThreads * V * N;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  vec16<T> *ring = reinterpret_cast<vec16<T> *>(smem_raw);  // [kPipeStages][TILE / N]
-  __shared__ __align__(8) unsigned long long bars[kPipeStages];
-  __shared__ uint32_t tile_of[kPipeStages];
-  __shared__ Acc warp_tot[kPipeWarps];
-  __shared__ Carry tile_prefix;
-  __shared__ int abort_flag;
-
-  const unsigned lane = lane_id();
-  const unsigned warp = threadIdx.x / kWarp;
-  auto issue = [&](int s, uint32_t t) {
-    const size_t first = size_t(t) * TILE;
-    const size_t cnt = (n - first) < size_t(TILE) ? (n - first) : size_t(TILE);
-    const uint32_t bytes = uint32_t(cnt * sizeof(T));
-    mbar_arrive_expect_tx(&bars[s], bytes);
-    bulk_load_smem(ring + size_t(s) * (TILE / N), in + first, bytes, &bars[s]);
-  };
-  if (threadIdx.x == 0) {
-    abort_flag = 0;
-    for (int s = 0; s < kPipeStages; ++s) mbar_init(&bars[s], 1);
-    fence_mbar_init();
-    fence_proxy_async_smem();
-    for (int s = 0; s < kPipeStages; ++s) {
-      const uint32_t t = atomicAdd(tile_counter, 1u);
-      tile_of[s] = t;
-      if (t < tiles) issue(s, t);
-    }
-  }
-  __syncthreads();
-
-  for (uint32_t it = 0;; ++it) {
-    const int s = int(it % kPipeStages);
-    const uint32_t parity = (it / kPipeStages) & 1u;
-    const uint32_t tile = tile_of[s];
-    if (tile >= tiles) break;
-    if (!mbar_wait_bounded(&bars[s], parity)) {
-      // A copy never completed: record it, give the outstanding copies a
-      // second bounded chance to land, and leave.
-      report_error(err, kErrPipeTimeout);
-      abort_flag = 1;
-    }
-    __syncthreads();
-    if (abort_flag) {
-      if (threadIdx.x == 0)
-        for (uint32_t j = 0; j < kPipeStages; ++j) {
-          const uint32_t it2 = it + j;
-          if (tile_of[it2 % kPipeStages] < tiles) mbar_wait_bounded(&bars[it2 % kPipeStages], (it2 / kPipeStages) & 1u);
-        }
-      return;
-    }
-    const size_t nv = n;  // no head padding: the kernel is only used on aligned data
-    const size_t tile_vec0 = size_t(tile) * kPipeThreads * V;
-    const size_t warp_vec = size_t(warp) * kWarp * V;
-    T x[V][N];
-    bool valid[V][N];
-#pragma unroll
-    for (int j = 0; j < V; ++j) {
-      const size_t lv = warp_vec + size_t(j) * kWarp + lane;  // vector index within the tile
-      const vec16<T> r = ring[size_t(s) * (TILE / N) + lv];
-#pragma unroll
-      for (int k = 0; k < N; ++k) {
-        x[j][k] = r.v[k];
-        valid[j][k] = (tile_vec0 + lv) * N + k < nv;
-      }
-    }
-    __syncthreads();  // every thread has its data: stage s may be refilled
-    if (threadIdx.x == 0) {
-      fence_proxy_async_smem();
-      const uint32_t t2 = atomicAdd(tile_counter, 1u);
-      tile_of[s] = t2;
-      if (t2 < tiles) issue(s, t2);
-    }
-    Acc lane_excl[V];
-    Acc chunk_pre[V];
-    Acc run = P::ident();
-#pragma unroll
-    for (int j = 0; j < V; ++j) {
-      Acc t = P::ident();
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        if (valid[j][k]) t = P::add(t, x[j][k]);
-      Acc incl = t;
-#pragma unroll
-      for (int d = 1; d < kWarp; d <<= 1) {
-        Acc o = P::shfl_up(incl, d);
-        if (int(lane) >= d) incl = P::comb(o, incl);
-      }
-      Acc ex = P::shfl_up(incl, 1);
-      lane_excl[j] = (lane == 0) ? P::ident() : ex;
-      chunk_pre[j] = run;
-      run = P::comb(run, P::shfl(incl, kWarp - 1));
-    }
-    if (lane == 0) warp_tot[warp] = run;
-    __syncthreads();
-    Acc warp_excl = P::ident();
-    Acc tile_agg = P::ident();
-#pragma unroll
-    for (int w = 0; w < kPipeWarps; ++w) {
-      if (w == int(warp)) warp_excl = tile_agg;
-      tile_agg = P::comb(tile_agg, warp_tot[w]);
-    }
-    if (warp == 0) {
-      const Carry first_prefix = exclusive ? init_carry : P::carry_ident();
-      Carry pre;
-      if (tile == 0) {
-        pre = first_prefix;
-        if (lane == 0) st.publish(0, kFlagPrefix, P::carry_comb(first_prefix, P::to_carry(tile_agg)));
-      } else {
-        pre = lookback<P>(st, tile, P::to_carry(tile_agg), err);
-      }
-      if (lane == 0) tile_prefix = pre;
-    }
-    __syncthreads();
-    const Acc base = P::comb(P::from_carry(tile_prefix), warp_excl);
-#pragma unroll
-    for (int j = 0; j < V; ++j) {
-      Acc r = P::comb(P::comb(base, chunk_pre[j]), lane_excl[j]);
-      vec16<T> w;
-#pragma unroll
-      for (int k = 0; k < N; ++k) {
-        if (exclusive) {
-          w.v[k] = P::out(r);
-          if (valid[j][k]) r = P::add(r, x[j][k]);
-        } else {
-          if (valid[j][k]) r = P::add(r, x[j][k]);
-          w.v[k] = P::out(r);
-        }
-      }
-      const size_t gv = tile_vec0 + warp_vec + size_t(j) * kWarp + lane;
-      if ((gv + 1) * N <= nv) st_stream16(reinterpret_cast<vec16<T> *>(out) + gv, w);
-      // (no partial vectors: n * sizeof(T) is a multiple of 16 on this path)
-    }
-  }
-}
-
 template <class T> struct scan_vectors_per_thread { static constexpr int value = 4; };
 
 template <class T, class P>
@@ -544,13 +402,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   const size_t tile_elems = size_t(kScanThreads) * V * N;
   const size_t tiles = div_up(nv, tile_elems);
   const bool single = (tiles <= 1);
-  // Pipelined kernel: aligned data, whole 16-byte vectors, more than one tile.
-  constexpr int kPipeV = scan_vectors_per_thread<T>::value;
-  const size_t pipe_tile = size_t(kPipeThreads) * kPipeV * N;
-  const size_t pipe_tiles = div_up(n, pipe_tile);
-  const bool pipe = !single && (ain % 16 == 0) && (aout % 16 == 0) && ((n * sizeof(T)) % 16 == 0) &&
-                    pipe_tiles > 1 && pipe_tiles < (size_t(1) << 31);
-  const size_t need = single ? 0 : (256 + Status::bytes(pipe ? (pipe_tiles > tiles ? pipe_tiles : tiles) : tiles));
+  const size_t need = single ? 0 : (256 + Status::bytes(tiles));
   TempStorage ts;
   bool query = false;
   rc = ts.acquire(temp, temp_bytes, need, s, &query);
@@ -569,28 +421,8 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   uint32_t *counter = reinterpret_cast<uint32_t *>(base);
   Status st;
   st.bind(base + 256, tiles);
-  BCX_CHECK(tiles < (size_t(1) << 31), BCX_INVALID_VALUE, "scan: input too large");
-  if (pipe) {
-    const size_t smem = size_t(kPipeStages) * kPipeThreads * kPipeV * 16;
-    static bool attr_set = false;
-    if (!attr_set) {
-      BCX_CUDA(cudaFuncSetAttribute(scan_pipe_kernel<T, P, kPipeV, Status>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-      attr_set = true;
-    }
-    int per_sm = 0;
-    BCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_pipe_kernel<T, P, kPipeV, Status>,
-                                                           kPipeThreads, smem));
-    if (per_sm < 1) per_sm = 1;
-    size_t grid = size_t(ds->sm_count) * size_t(per_sm);
-    if (grid > pipe_tiles) grid = pipe_tiles;
-    BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(pipe_tiles), s));
-    KernelScope ks("scan_lookback", s);
-    scan_pipe_kernel<T, P, kPipeV, Status><<<unsigned(grid), kPipeThreads, smem, s>>>(
-        pin, pout, n, exclusive, init_carry, st, counter, uint32_t(pipe_tiles), ds->err_word);
-    return launch_status("scan_lookback");
-  }
   BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
+  BCX_CHECK(tiles < (size_t(1) << 31), BCX_INVALID_VALUE, "scan: input too large");
   KernelScope ks("scan_lookback", s);
   scan_tile_kernel<T, P, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
       pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);

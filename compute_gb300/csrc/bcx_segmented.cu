@@ -1,0 +1,444 @@
+// bcx_segmented.cu -- segmented scan and segmented reduce in one launch each.
+//
+// The reference has no segmented algorithms: a caller loops over segments and
+// issues one exclusive_scan / reduce per segment (each several launches, see
+// algorithm/detail/scan_on_gpu.hpp:187-267 and reduce_on_gpu.hpp:169-280), or
+// uses reduce_by_key with segment ids as keys (reduce_by_key_with_scan.hpp).
+// Segments here are CSR offsets: segment s is [offsets[s], offsets[s+1]),
+// offsets[0] == 0, offsets[nseg] == n, non-decreasing (empty segments allowed).
+//
+// Segmented scan: the decoupled look-back scan with the segmented operator
+// (head, value): (a then b) = (a.head | b.head, b.head ? b.value : a op b).
+// Each tile marks the segment heads that fall inside it in a shared-memory
+// bitmap (one binary search per tile, then one pass over those offsets), so a
+// tile costs one read and one write of its elements whatever the segment
+// sizes.  Exclusive scans start every segment at init.
+//
+// Segmented reduce: persistent blocks take segments from a ticket counter and
+// fold each with every thread striding the segment, four independent
+// accumulators per thread; one output per segment (init for an empty one).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <type_traits>
+
+#include "bcx.h"
+#include "bcx_common.cuh"
+#include "bcx_internal.h"
+
+namespace bcx {
+namespace {
+
+constexpr int kSegThreads = 256;
+constexpr int kSegWarps = kSegThreads / kWarp;
+constexpr int kSegItems = 8;
+constexpr int kSegTile = kSegThreads * kSegItems;
+enum : uint32_t { kSgInvalid = 0, kSgAggregate = 1, kSgPrefix = 2 };
+
+template <class T, template <class> class OpT>
+struct SgPlain {
+  typedef typename widen<T>::type Acc;
+  typedef OpT<Acc> Op;
+  __device__ __forceinline__ static Acc ident() { return Op::identity(); }
+  __device__ __forceinline__ static Acc from(T x) { return Acc(x); }
+  __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return Op()(a, b); }
+  __device__ __forceinline__ static T out(Acc a) { return T(a); }
+  __device__ __forceinline__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static Acc shfl_down(Acc a, int d) { return __shfl_down_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static Acc shfl(Acc a, int s) { return __shfl_sync(0xffffffffu, a, s); }
+};
+struct SgCompF32 {
+  typedef comp_f32 Acc;
+  __device__ __forceinline__ static Acc ident() { return comp_f32{0.f, 0.f}; }
+  __device__ __forceinline__ static Acc from(float x) { return comp_f32{x, 0.f}; }
+  __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return comp_merge(a, b); }
+  __device__ __forceinline__ static float out(Acc a) { return a.s + a.c; }
+  __device__ __forceinline__ static Acc shfl_up(Acc a, int d) {
+    return comp_f32{__shfl_up_sync(0xffffffffu, a.s, d), __shfl_up_sync(0xffffffffu, a.c, d)};
+  }
+  __device__ __forceinline__ static Acc shfl_down(Acc a, int d) {
+    return comp_f32{__shfl_down_sync(0xffffffffu, a.s, d), __shfl_down_sync(0xffffffffu, a.c, d)};
+  }
+  __device__ __forceinline__ static Acc shfl(Acc a, int s) {
+    return comp_f32{__shfl_sync(0xffffffffu, a.s, s), __shfl_sync(0xffffffffu, a.c, s)};
+  }
+};
+
+// (head flag, value); combine is "b restarts the segment if it holds a head".
+template <class P>
+struct Sg {
+  uint32_t h;
+  typename P::Acc v;
+};
+template <class P>
+__device__ __forceinline__ Sg<P> sg_comb(const Sg<P> &a, const Sg<P> &b) {
+  return Sg<P>{a.h | b.h, b.h ? b.v : P::comb(a.v, b.v)};
+}
+template <class P>
+__device__ __forceinline__ Sg<P> sg_ident() {
+  return Sg<P>{0u, P::ident()};
+}
+template <class P>
+__device__ __forceinline__ Sg<P> sg_shfl_up(const Sg<P> &a, int d) {
+  return Sg<P>{__shfl_up_sync(0xffffffffu, a.h, d), P::shfl_up(a.v, d)};
+}
+template <class P>
+__device__ __forceinline__ Sg<P> sg_shfl_down(const Sg<P> &a, int d) {
+  return Sg<P>{__shfl_down_sync(0xffffffffu, a.h, d), P::shfl_down(a.v, d)};
+}
+template <class P>
+__device__ __forceinline__ Sg<P> sg_shfl(const Sg<P> &a, int s) {
+  return Sg<P>{__shfl_sync(0xffffffffu, a.h, s), P::shfl(a.v, s)};
+}
+
+template <class P>
+struct SgStatus {
+  uint32_t *flags;
+  Sg<P> *agg;
+  Sg<P> *inc;
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, const Sg<P> &v) {
+    if (flag == kSgAggregate) agg[t] = v;
+    else inc[t] = v;
+    st_release_u32(&flags[t], flag);
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, Sg<P> *v) const {
+    const uint32_t f = ld_acquire_u32(&flags[t]);
+    if (f != kSgInvalid) {
+      const Sg<P> *src = (f == kSgAggregate) ? &agg[t] : &inc[t];
+      const volatile uint32_t *w = reinterpret_cast<const volatile uint32_t *>(src);
+      uint32_t tmp[sizeof(Sg<P>) / 4];
+#pragma unroll
+      for (int i = 0; i < int(sizeof(Sg<P>) / 4); ++i) tmp[i] = w[i];
+      memcpy(v, tmp, sizeof(Sg<P>));
+    }
+    return f;
+  }
+};
+
+// Index of the first offset >= x among offsets[0..count).
+__device__ __forceinline__ size_t lower_bound_u64(const unsigned long long *offsets, size_t count,
+                                                  unsigned long long x) {
+  size_t lo = 0, hi = count;
+  while (lo < hi) {
+    const size_t mid = (lo + hi) / 2;
+    if (offsets[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <class T, class P>
+__global__ void __launch_bounds__(kSegThreads)
+segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
+                      const unsigned long long *__restrict__ offsets, size_t nseg, int exclusive,
+                      typename P::Acc init, SgStatus<P> st, uint32_t *__restrict__ tile_counter,
+                      uint32_t *err) {
+  typedef Sg<P> S;
+  __shared__ uint32_t s_heads[kSegTile / 32];
+  __shared__ S s_warp[kSegWarps];
+  __shared__ S s_prefix;
+  __shared__ uint32_t s_tile;
+  const unsigned lane = lane_id(), warp = threadIdx.x / kWarp;
+  for (int i = threadIdx.x; i < kSegTile / 32; i += kSegThreads) s_heads[i] = 0;
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+  __syncthreads();
+  const size_t tile = s_tile;
+  const size_t tile_base = tile * kSegTile;
+  const size_t tile_end = (tile_base + kSegTile < n) ? tile_base + kSegTile : n;
+  // Mark the segment starts inside this tile (offsets[0..nseg] are starts;
+  // offsets[nseg] == n is not).
+  if (warp == 0) {
+    const size_t first = lower_bound_u64(offsets, nseg, tile_base);
+    for (size_t k = first + lane; k < nseg; k += kWarp) {
+      const unsigned long long o = offsets[k];
+      if (o >= tile_end) break;
+      const uint32_t local = uint32_t(o - tile_base);
+      atomicOr(&s_heads[local >> 5], 1u << (local & 31u));
+    }
+  }
+  __syncthreads();
+  const uint32_t warp_first = warp * (kWarp * kSegItems);
+  T x[kSegItems];
+#pragma unroll
+  for (int i = 0; i < kSegItems; ++i) {
+    const size_t idx = tile_base + warp_first + i * kWarp + lane;
+    x[i] = idx < n ? in[idx] : T(0);
+  }
+  S lane_incl[kSegItems];
+  S run = sg_ident<P>();
+#pragma unroll
+  for (int i = 0; i < kSegItems; ++i) {
+    const uint32_t local = warp_first + i * kWarp + lane;
+    const size_t idx = tile_base + local;
+    S e;
+    e.h = (s_heads[local >> 5] >> (local & 31u)) & 1u;
+    e.v = idx < n ? P::from(x[i]) : P::ident();
+#pragma unroll
+    for (int d = 1; d < kWarp; d <<= 1) {
+      const S o = sg_shfl_up<P>(e, d);
+      if (int(lane) >= d) e = sg_comb<P>(o, e);
+    }
+    lane_incl[i] = e;
+    run = sg_comb<P>(run, sg_shfl<P>(e, kWarp - 1));
+  }
+  if (lane == 0) s_warp[warp] = run;
+  __syncthreads();
+  S warp_excl = sg_ident<P>(), tile_agg = sg_ident<P>();
+#pragma unroll
+  for (int w = 0; w < kSegWarps; ++w) {
+    if (w == int(warp)) warp_excl = tile_agg;
+    tile_agg = sg_comb<P>(tile_agg, s_warp[w]);
+  }
+  if (warp == 0) {
+    S excl = sg_ident<P>();
+    if (tile == 0) {
+      if (lane == 0) st.publish(0, kSgPrefix, tile_agg);
+    } else {
+      if (lane == 0) st.publish(tile, kSgAggregate, tile_agg);
+      long long pred = (long long)tile - 1;
+      bool gave_up = false;
+      while (true) {
+        const long long t = pred - (long long)lane;
+        S val = sg_ident<P>();
+        uint32_t f = kSgPrefix;
+        if (t >= 0) {
+          uint32_t spins = 0;
+          f = st.poll(size_t(t), &val);
+          while (f == kSgInvalid) {
+            if (++spins > kSpinLimit) {
+              gave_up = true;
+              f = kSgPrefix;
+              val = sg_ident<P>();
+              break;
+            }
+            if (spins > 16) __nanosleep(64);
+            f = st.poll(size_t(t), &val);
+          }
+        }
+        const unsigned pmask = __ballot_sync(0xffffffffu, f == kSgPrefix);
+        const int firstp = pmask ? __ffs(pmask) - 1 : kWarp - 1;
+        if (int(lane) > firstp) val = sg_ident<P>();
+#pragma unroll
+        for (int d = 1; d < kWarp; d <<= 1) {
+          const S o = sg_shfl_down<P>(val, d);
+          if (int(lane) + d < kWarp) val = sg_comb<P>(o, val);
+        }
+        excl = sg_comb<P>(sg_shfl<P>(val, 0), excl);
+        if (pmask) break;
+        pred -= kWarp;
+      }
+      if (__any_sync(0xffffffffu, gave_up) && lane == 0) report_error(err, kErrLookbackTimeout);
+      if (lane == 0) st.publish(tile, kSgPrefix, sg_comb<P>(excl, tile_agg));
+    }
+    if (lane == 0) s_prefix = excl;
+  }
+  __syncthreads();
+  // Inclusive value of every element; the exclusive output of element i is
+  // init op (inclusive of i-1 if i continues a segment).
+  S pre = sg_comb<P>(s_prefix, warp_excl);
+  typename P::Acc prev_last = P::ident();  // inclusive value of the element before item i, lane 0
+  uint32_t prev_last_valid = 0;
+  {
+    // the element before this warp's first item: the tile/warp prefix itself
+    prev_last = pre.v;
+    prev_last_valid = 1;
+  }
+#pragma unroll
+  for (int i = 0; i < kSegItems; ++i) {
+    const uint32_t local = warp_first + i * kWarp + lane;
+    const size_t idx = tile_base + local;
+    const S incl = sg_comb<P>(pre, lane_incl[i]);
+    if (exclusive) {
+      typename P::Acc before = P::shfl_up(incl.v, 1);
+      if (lane == 0) before = prev_last;
+      const uint32_t h = (s_heads[local >> 5] >> (local & 31u)) & 1u;
+      const typename P::Acc e = (h || (lane == 0 && !prev_last_valid)) ? init : P::comb(init, before);
+      if (idx < n) out[idx] = P::out(e);
+    } else {
+      if (idx < n) out[idx] = P::out(incl.v);
+    }
+    prev_last = P::shfl(incl.v, kWarp - 1);
+    pre = sg_comb<P>(pre, sg_shfl<P>(lane_incl[i], kWarp - 1));
+  }
+}
+
+template <class T, class P>
+__global__ void __launch_bounds__(kSegThreads)
+segmented_reduce_kernel(const T *__restrict__ in, const unsigned long long *__restrict__ offsets, size_t nseg,
+                        typename P::Acc init, T *__restrict__ out, uint32_t *__restrict__ seg_counter) {
+  typedef typename P::Acc Acc;
+  __shared__ Acc s_acc[kSegWarps];
+  __shared__ uint32_t s_seg;
+  while (true) {
+    if (threadIdx.x == 0) s_seg = atomicAdd(seg_counter, 1u);
+    __syncthreads();
+    const size_t seg = s_seg;
+    if (seg >= nseg) break;
+    const size_t b = offsets[seg], e = offsets[seg + 1];
+    Acc a0 = P::ident(), a1 = P::ident(), a2 = P::ident(), a3 = P::ident();
+    size_t i = b + threadIdx.x;
+    for (; i + 3 * kSegThreads < e; i += 4 * kSegThreads) {
+      const T x0 = in[i], x1 = in[i + kSegThreads], x2 = in[i + 2 * kSegThreads], x3 = in[i + 3 * kSegThreads];
+      a0 = P::comb(a0, P::from(x0));
+      a1 = P::comb(a1, P::from(x1));
+      a2 = P::comb(a2, P::from(x2));
+      a3 = P::comb(a3, P::from(x3));
+    }
+    for (; i < e; i += kSegThreads) a0 = P::comb(a0, P::from(in[i]));
+    Acc a = P::comb(P::comb(a0, a1), P::comb(a2, a3));
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) a = P::comb(a, P::shfl_down(a, d));
+    if (lane_id() == 0) s_acc[threadIdx.x / kWarp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      Acc r = init;
+      for (int w = 0; w < kSegWarps; ++w) r = P::comb(r, s_acc[w]);
+      out[seg] = P::out(r);
+    }
+    __syncthreads();
+  }
+}
+
+template <class T, class P>
+bcx_status run_segmented_scan(cudaStream_t s, int exclusive, const void *init, const void *in, void *out,
+                              size_t n, const unsigned long long *offsets, size_t nseg, void *temp,
+                              size_t *temp_bytes) {
+  typedef Sg<P> S;
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
+  const size_t tiles = div_up(n, kSegTile);
+  const size_t need = 256 + align256(tiles * 4) + 2 * align256(tiles * sizeof(S));
+  TempStorage ts;
+  bool query = false;
+  rc = ts.acquire(temp, temp_bytes, need, s, &query);
+  if (rc || query) return rc;
+  char *base = static_cast<char *>(ts.ptr());
+  SgStatus<P> st;
+  st.flags = reinterpret_cast<uint32_t *>(base + 256);
+  st.agg = reinterpret_cast<S *>(base + 256 + align256(tiles * 4));
+  st.inc = reinterpret_cast<S *>(base + 256 + align256(tiles * 4) + align256(tiles * sizeof(S)));
+  BCX_CUDA(cudaMemsetAsync(base, 0, 256 + align256(tiles * 4), s));
+  T init_v;
+  memcpy(&init_v, init, sizeof(T));
+  KernelScope ks("segmented_scan", s);
+  segmented_scan_kernel<T, P><<<unsigned(tiles), kSegThreads, 0, s>>>(
+      static_cast<const T *>(in), static_cast<T *>(out), n, offsets, nseg, exclusive, P::from_host(init_v), st,
+      reinterpret_cast<uint32_t *>(base), ds->err_word);
+  return launch_status("segmented_scan");
+}
+
+template <class T, class P>
+bcx_status run_segmented_reduce(cudaStream_t s, const void *in, const unsigned long long *offsets, size_t nseg,
+                                const void *init, void *out, void *temp, size_t *temp_bytes) {
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
+  TempStorage ts;
+  bool query = false;
+  rc = ts.acquire(temp, temp_bytes, 256, s, &query);
+  if (rc || query) return rc;
+  BCX_CUDA(cudaMemsetAsync(ts.ptr(), 0, 256, s));
+  T init_v;
+  memcpy(&init_v, init, sizeof(T));
+  size_t blocks = size_t(ds->sm_count) * 8;
+  if (blocks > nseg) blocks = nseg;
+  KernelScope ks("segmented_reduce", s);
+  segmented_reduce_kernel<T, P><<<unsigned(blocks), kSegThreads, 0, s>>>(
+      static_cast<const T *>(in), offsets, nseg, P::from_host(init_v), static_cast<T *>(out),
+      static_cast<uint32_t *>(ts.ptr()));
+  return launch_status("segmented_reduce");
+}
+
+// Host-side conversion of init into the accumulator type.
+template <class T, template <class> class OpT>
+struct SgPlainH : SgPlain<T, OpT> {
+  static typename SgPlain<T, OpT>::Acc from_host(T v) { return typename SgPlain<T, OpT>::Acc(v); }
+};
+struct SgCompF32H : SgCompF32 {
+  static comp_f32 from_host(float v) { return comp_f32{v, 0.f}; }
+};
+
+template <class T, class Fn>
+bcx_status seg_dispatch_op(int op, int comp, Fn &&fn) {
+  switch (op) {
+    case BCX_PLUS:
+      if constexpr (sizeof(T) == 4 && type_traits<T>::is_float) {
+        if (comp) return fn(static_cast<SgCompF32H *>(nullptr));
+      }
+      return fn(static_cast<SgPlainH<T, op_plus> *>(nullptr));
+    case BCX_MULTIPLIES: return fn(static_cast<SgPlainH<T, op_multiplies> *>(nullptr));
+    case BCX_MIN: return fn(static_cast<SgPlainH<T, op_min> *>(nullptr));
+    case BCX_MAX: return fn(static_cast<SgPlainH<T, op_max> *>(nullptr));
+  }
+  return BCX_UNSUPPORTED;
+}
+
+template <class Fn>
+bcx_status seg_dispatch(bcx_dtype t, int op, int comp, Fn &&fn) {
+  switch (t) {
+    case BCX_INT: return seg_dispatch_op<int32_t>(op, comp, [&](auto *p) { return fn((int32_t *)nullptr, p); });
+    case BCX_UINT: return seg_dispatch_op<uint32_t>(op, comp, [&](auto *p) { return fn((uint32_t *)nullptr, p); });
+    case BCX_LONG: return seg_dispatch_op<long long>(op, comp, [&](auto *p) { return fn((long long *)nullptr, p); });
+    case BCX_ULONG:
+      return seg_dispatch_op<unsigned long long>(op, comp, [&](auto *p) { return fn((unsigned long long *)nullptr, p); });
+    case BCX_FLOAT: return seg_dispatch_op<float>(op, comp, [&](auto *p) { return fn((float *)nullptr, p); });
+    case BCX_DOUBLE: return seg_dispatch_op<double>(op, comp, [&](auto *p) { return fn((double *)nullptr, p); });
+    default: break;
+  }
+  return BCX_UNSUPPORTED;
+}
+
+}  // namespace
+}  // namespace bcx
+
+using namespace bcx;
+
+extern "C" {
+
+bcx_status bcx_segmented_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive, const void *init,
+                              const void *in, void *out, size_t n, const uint64_t *offsets, size_t nseg,
+                              int compensated, void *temp, size_t *temp_bytes) {
+  clear_error();
+  BCX_CHECK(dtype_valid(type), BCX_INVALID_VALUE, "invalid dtype %d", int(type));
+  if (n == 0) {
+    if (temp == nullptr && temp_bytes != nullptr) *temp_bytes = 0;
+    return BCX_SUCCESS;
+  }
+  BCX_CHECK(in && out && offsets && nseg > 0, BCX_INVALID_VALUE, "NULL argument or no segments");
+  BCX_CHECK(n < (size_t(1) << 40), BCX_INVALID_VALUE, "segmented scan: n too large");
+  unsigned char zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const void *init_p = (exclusive && init) ? init : zero;
+  const auto *offs = reinterpret_cast<const unsigned long long *>(offsets);
+  bcx_status rc = seg_dispatch(type, op, compensated, [&](auto *tp, auto *pp) -> bcx_status {
+    typedef std::remove_pointer_t<decltype(tp)> T;
+    typedef std::remove_pointer_t<decltype(pp)> P;
+    return run_segmented_scan<T, P>((cudaStream_t)stream, exclusive, init_p, in, out, n, offs, nseg, temp,
+                                    temp_bytes);
+  });
+  if (rc == BCX_UNSUPPORTED) set_error("segmented scan: dtype %d / functor %d not provided", int(type), int(op));
+  return rc;
+}
+
+bcx_status bcx_segmented_reduce(bcx_stream stream, bcx_dtype type, bcx_op op, const void *in,
+                                const uint64_t *offsets, size_t nseg, const void *init, void *out,
+                                int compensated, void *temp, size_t *temp_bytes) {
+  clear_error();
+  BCX_CHECK(dtype_valid(type), BCX_INVALID_VALUE, "invalid dtype %d", int(type));
+  if (nseg == 0) {
+    if (temp == nullptr && temp_bytes != nullptr) *temp_bytes = 0;
+    return BCX_SUCCESS;
+  }
+  BCX_CHECK(in && offsets && out && init, BCX_INVALID_VALUE, "NULL argument");
+  const auto *offs = reinterpret_cast<const unsigned long long *>(offsets);
+  bcx_status rc = seg_dispatch(type, op, compensated, [&](auto *tp, auto *pp) -> bcx_status {
+    typedef std::remove_pointer_t<decltype(tp)> T;
+    typedef std::remove_pointer_t<decltype(pp)> P;
+    return run_segmented_reduce<T, P>((cudaStream_t)stream, in, offs, nseg, init, out, temp, temp_bytes);
+  });
+  if (rc == BCX_UNSUPPORTED)
+    set_error("segmented reduce: dtype %d / functor %d not provided", int(type), int(op));
+  return rc;
+}
+
+}  // extern "C"

@@ -212,6 +212,26 @@ bcx_status bcx_reduce_by_key(bcx_stream stream, bcx_dtype key_type,
                              uint64_t *num_runs_dev, int compensated,
                              void *temp, size_t *temp_bytes);
 
+/* ---- segmented algorithms ------------------------------------------------
+ * No reference counterpart as one call: the reference's callers loop over
+ * segments with one exclusive_scan / reduce each (scan_on_gpu.hpp:187-267,
+ * reduce_on_gpu.hpp:169-280) or use reduce_by_key with segment ids
+ * (reduce_by_key_with_scan.hpp:432-486).  Segments are CSR offsets in device
+ * memory: nseg + 1 uint64 values, offsets[0] == 0, offsets[nseg] == n,
+ * non-decreasing (empty segments allowed).  Types int/uint/long/ulong/float/
+ * double; functors plus, multiplies, min, max.  One kernel launch each. */
+/* Scan restarted at every segment start (exclusive: each segment starts at
+ * *init). */
+bcx_status bcx_segmented_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive,
+                              const void *init, const void *in, void *out, size_t n,
+                              const uint64_t *offsets, size_t nseg, int compensated,
+                              void *temp, size_t *temp_bytes);
+/* out[s] = *init op fold(in[offsets[s] .. offsets[s+1])) for each segment
+ * (*init for an empty segment). */
+bcx_status bcx_segmented_reduce(bcx_stream stream, bcx_dtype type, bcx_op op, const void *in,
+                                const uint64_t *offsets, size_t nseg, const void *init, void *out,
+                                int compensated, void *temp, size_t *temp_bytes);
+
 /* ---- run-time compiled kernels ------------------------------------------
  * Replaces clBuildProgram + program_cache (utility/program_cache.hpp:52-168,
  * program.hpp:638-692) and the offline binary cache (program.hpp:656-690):

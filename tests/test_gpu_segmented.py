@@ -1,0 +1,102 @@
+"""Segmented scan / reduce (one launch each) against per-segment oracle calls.
+
+Segments are CSR offsets; the equivalent reference code is one plain call
+per segment, so each segment's result must equal the oracle on that slice
+(bit-exact for integers, FP64-oracle tolerance for compensated floats)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+NP = {"int": np.int32, "uint": np.uint32, "long": np.int64, "ulong": np.uint64, "float": np.float32,
+      "double": np.float64}
+TORCH_NP = {"int": np.int32, "uint": np.int32, "long": np.int64, "ulong": np.int64, "float": np.float32,
+            "double": np.float64}
+
+
+def log_uniform_offsets(rng, nseg, lo, hi, empty_frac=0.0):
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), size=nseg)).astype(np.int64)
+    if empty_frac:
+        sizes[rng.random(nseg) < empty_frac] = 0
+    return np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+
+
+def run_seg_scan(torch, x, dtype, op, exclusive, init, offsets):
+    from compute_gb300 import _lib
+    lib = _lib.lib()
+    d = torch.from_numpy(x.view(TORCH_NP[dtype]).copy()).cuda()
+    out = torch.empty_like(d)
+    offs = torch.from_numpy(offsets.view(np.int64).copy()).cuda()
+    init_b = np.array([init], dtype=NP[dtype])
+    rc = lib.bcx_segmented_scan(torch.cuda.current_stream().cuda_stream, _lib.DTYPES[dtype], _lib.OPS[op],
+                                int(exclusive), init_b.ctypes.data_as(ctypes.c_void_p), d.data_ptr(),
+                                out.data_ptr(), x.size, offs.data_ptr(), offsets.size - 1, 1, None, None)
+    assert rc == 0, lib.bcx_last_error_string()
+    return out.cpu().numpy().view(NP[dtype])
+
+
+@pytest.mark.parametrize("dtype", ["int", "uint", "long", "float"])
+@pytest.mark.parametrize("op", ["plus", "max"])
+@pytest.mark.parametrize("exclusive", [False, True])
+def test_segmented_scan_matches_per_segment(cuda, dtype, op, exclusive):
+    rng = np.random.default_rng(3)
+    offsets = log_uniform_offsets(rng, 700, 1, 20000, empty_frac=0.05)
+    n = int(offsets[-1])
+    if dtype == "float":
+        x = rng.integers(-100, 100, size=n).astype(np.float32)  # exact in FP32: order does not matter
+    else:
+        x = rng.integers(0, 1000, size=n).astype(NP[dtype])
+    init = 5
+    got = run_seg_scan(cuda, x, dtype, op, exclusive, init, offsets)
+    for s in range(offsets.size - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        if a == b:
+            continue
+        ref = oracle.scan(x[a:b], dtype, op=op, exclusive=exclusive, init=init)
+        np.testing.assert_array_equal(got[a:b], ref, err_msg=f"segment {s} [{a},{b})")
+
+
+def test_segmented_scan_float_compensated_accuracy(cuda):
+    rng = np.random.default_rng(8)
+    offsets = log_uniform_offsets(rng, 60, 16, 1 << 18)
+    n = int(offsets[-1])
+    x = rng.standard_normal(n).astype(np.float32)
+    got = run_seg_scan(cuda, x, "float", "plus", False, 0, offsets).astype(np.float64)
+    for s in range(offsets.size - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        ref = oracle.prefix_f64(x[a:b], "float")
+        bound = np.cumsum(np.abs(x[a:b]).astype(np.float64)) * 2.0 ** -23 * 2 + 1e-30
+        assert (np.abs(got[a:b] - ref) <= bound).all(), s
+
+
+@pytest.mark.parametrize("dtype", ["int", "ulong", "float", "double"])
+@pytest.mark.parametrize("op", ["plus", "min"])
+def test_segmented_reduce_matches_per_segment(cuda, dtype, op):
+    from compute_gb300 import _lib
+    lib = _lib.lib()
+    torch = cuda
+    rng = np.random.default_rng(4)
+    offsets = log_uniform_offsets(rng, 2000, 1, 1 << 16, empty_frac=0.02)
+    n = int(offsets[-1])
+    x = rng.integers(-1000, 1000, size=n).astype(NP[dtype]) if dtype not in ("ulong",) else \
+        rng.integers(0, 1000, size=n).astype(np.uint64)
+    d = torch.from_numpy(x.view(TORCH_NP[dtype]).copy()).cuda()
+    offs = torch.from_numpy(offsets.view(np.int64).copy()).cuda()
+    out = torch.empty(offsets.size - 1, dtype=d.dtype, device="cuda")
+    init = np.array([7 if op == "plus" else 10**6], dtype=NP[dtype])
+    rc = lib.bcx_segmented_reduce(torch.cuda.current_stream().cuda_stream, _lib.DTYPES[dtype], _lib.OPS[op],
+                                  d.data_ptr(), offs.data_ptr(), offsets.size - 1,
+                                  init.ctypes.data_as(ctypes.c_void_p), out.data_ptr(), 1, None, None)
+    assert rc == 0, lib.bcx_last_error_string()
+    got = out.cpu().numpy().view(NP[dtype])
+    for s in range(offsets.size - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        ref = oracle.fold(x[a:b], dtype, op=op, init=init[0])
+        if dtype in ("float", "double") and op == "plus":
+            assert got[s] == NP[dtype](oracle.sum_f64(x[a:b], dtype, init=float(init[0]))), s
+        else:
+            assert got[s] == ref, (s, got[s], ref)
