@@ -68,6 +68,7 @@ SIGNATURES = {
     "bcx_reduce_by_key": (_i, [_vp, _i, _i, _i, _vp, _vp, _sz, _vp, _vp, _vp, _i, _vp, _szp]),
     "bcx_segmented_scan": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp, _sz, _i, _vp, _szp]),
     "bcx_segmented_reduce": (_i, [_vp, _i, _i, _vp, _vp, _sz, _vp, _vp, _i, _vp, _szp]),
+    "bcx_segmented_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _vp, _sz, _i, _vp, _szp]),
     "bcx_jit_get_kernel": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(_vp)]),
     "bcx_jit_launch": (_i, [_vp, C.c_uint, C.c_uint, _sz, _vp, C.POINTER(_vp)]),
     "bcx_jit_build_log": (_i, [C.c_char_p, _sz, _szp]),

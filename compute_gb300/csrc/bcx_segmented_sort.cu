@@ -1,0 +1,537 @@
+// bcx_segmented_sort.cu -- segmented sort / sort_by_key as one stream of
+// kernels (graph-capturable: nothing is read back to the host).
+//
+// The reference has no segmented sort: a caller sorts each segment with its
+// own sort_by_key call (sort_by_key.hpp:33-163 -> radix_sort.hpp:253-426,
+// ~6 launches per 4-bit pass).  Here segments are CSR offsets (device
+// memory, nseg + 1 uint64, offsets[0] == 0, offsets[nseg] == n) and every
+// segment is sorted stably and independently, in the reference's radix order
+// (the same key transform as the plain sort).
+//
+// Small segments (up to a few thousand pairs) are sorted by one block each,
+// entirely in shared memory: load once, one stable 8-bit LSD pass per digit
+// between two shared-memory buffers (passes whose digit is the same for the
+// whole segment are skipped), store once.
+//
+// Large segments are cut into tiles that never cross a segment boundary and
+// sorted with the onesweep tile routine of the plain sort: a device-side plan
+// numbers the tiles, one kernel builds every large segment's digit
+// histograms, one turns them into per-segment digit start offsets, and one
+// kernel per digit pass moves the tiles, each tile looking back only over the
+// tiles of its own segment.
+#include <cuda_runtime.h>
+
+#include "bcx.h"
+#include "bcx_common.cuh"
+#include "bcx_internal.h"
+#include "bcx_radix.cuh"
+
+namespace bcx {
+namespace {
+
+using namespace radix;
+
+constexpr int kPlanThreads = 1024;
+
+// Largest segment the shared-memory path sorts: about 96 KB of double
+// buffered keys and values, at most 4096 pairs.
+template <class U, int VB>
+struct SmallCap {
+  typedef typename value_type_of<VB>::type VT;
+  static constexpr size_t kPair = sizeof(U) + (VB ? sizeof(VT) : 0);
+  static constexpr int raw = int((96 * 1024) / (2 * kPair));
+  static constexpr int value = raw >= 4096 ? 4096 : (raw >= 2048 ? 2048 : 1024);
+  static constexpr int IPT = value / kSortThreads;
+  static constexpr size_t kBytes = size_t(kSortWarps) * kRadix * 4 + 2 * size_t(value) * kPair;
+};
+
+// ---- plan ------------------------------------------------------------------
+// tile_first[s]: first large tile of segment s (exclusive scan of tile counts,
+// tile_first[nseg] = total tiles); large_ord[s]: ordinal of s among the large
+// segments; seg_of_large[k]: segment of the k-th large segment;
+// totals[0] = large tiles, totals[1] = large segments.
+__global__ void __launch_bounds__(kPlanThreads)
+segsort_plan_kernel(const unsigned long long *__restrict__ offsets, uint32_t nseg, uint32_t small_cap,
+                    uint32_t tile, uint32_t *__restrict__ tile_first, uint32_t *__restrict__ large_ord,
+                    uint32_t *__restrict__ seg_of_large, uint32_t *__restrict__ totals) {
+  __shared__ uint32_t warp_t[kPlanThreads / kWarp], warp_l[kPlanThreads / kWarp];
+  __shared__ uint32_t carry_t, carry_l;
+  const unsigned lane = lane_id(), warp = threadIdx.x / kWarp;
+  if (threadIdx.x == 0) carry_t = carry_l = 0;
+  __syncthreads();
+  for (uint32_t b = 0; b < nseg; b += kPlanThreads) {
+    const uint32_t s = b + threadIdx.x;
+    uint32_t t = 0, l = 0;
+    if (s < nseg) {
+      const unsigned long long len = offsets[s + 1] - offsets[s];
+      if (len > small_cap) {
+        l = 1;
+        t = uint32_t((len + tile - 1) / tile);
+      }
+    }
+    uint32_t it = t, il = l;
+#pragma unroll
+    for (int d = 1; d < kWarp; d <<= 1) {
+      const uint32_t ot = __shfl_up_sync(0xffffffffu, it, d), ol = __shfl_up_sync(0xffffffffu, il, d);
+      if (int(lane) >= d) {
+        it += ot;
+        il += ol;
+      }
+    }
+    if (lane == kWarp - 1) {
+      warp_t[warp] = it;
+      warp_l[warp] = il;
+    }
+    __syncthreads();
+    uint32_t bt = carry_t, bl = carry_l;
+    for (unsigned w = 0; w < warp; ++w) {
+      bt += warp_t[w];
+      bl += warp_l[w];
+    }
+    if (s < nseg) {
+      tile_first[s] = bt + it - t;
+      large_ord[s] = bl + il - l;
+      if (l) seg_of_large[bl + il - l] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == kPlanThreads - 1) {
+      carry_t = bt + it;
+      carry_l = bl + il;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    tile_first[nseg] = carry_t;
+    totals[0] = carry_t;
+    totals[1] = carry_l;
+  }
+}
+
+// Segment holding large tile t: the last s with tile_first[s] <= t among the
+// segments that own tiles.
+__device__ __forceinline__ uint32_t segment_of_tile(const uint32_t *__restrict__ tile_first, uint32_t nseg,
+                                                    uint32_t t) {
+  uint32_t lo = 0, hi = nseg;  // find last s with tile_first[s] <= t and tile_first[s+1] > t
+  while (lo + 1 < hi) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (tile_first[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  // skip segments without tiles that share the same tile_first
+  while (lo + 1 < nseg && tile_first[lo + 1] <= t) ++lo;
+  return lo;
+}
+
+struct LargeTile {
+  uint32_t seg, ord, base, count, first_tile;
+};
+
+template <class U>
+__device__ __forceinline__ LargeTile locate_tile(const unsigned long long *__restrict__ offsets,
+                                                 const uint32_t *__restrict__ tile_first,
+                                                 const uint32_t *__restrict__ large_ord, uint32_t nseg, uint32_t t,
+                                                 uint32_t tile) {
+  LargeTile r;
+  r.seg = segment_of_tile(tile_first, nseg, t);
+  r.ord = large_ord[r.seg];
+  r.first_tile = tile_first[r.seg];
+  const unsigned long long b = offsets[r.seg], e = offsets[r.seg + 1];
+  r.base = uint32_t(b + (unsigned long long)(t - r.first_tile) * tile);
+  const unsigned long long left = e - r.base;
+  r.count = uint32_t(left < tile ? left : tile);
+  return r;
+}
+
+// ---- large segments: histograms and digit starts --------------------------
+template <class U, int PASSES>
+__global__ void __launch_bounds__(kHistThreads)
+segsort_hist_kernel(const U *__restrict__ keys, const unsigned long long *__restrict__ offsets, uint32_t nseg,
+                    const uint32_t *__restrict__ tile_first, const uint32_t *__restrict__ large_ord,
+                    const uint32_t *__restrict__ totals, uint32_t tile, const KeyXform<U> xf,
+                    uint32_t *__restrict__ seg_hist) {
+  __shared__ uint32_t sh[PASSES][kRadix];
+  const uint32_t t = blockIdx.x;
+  if (t >= totals[0]) return;
+  for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
+  __syncthreads();
+  const LargeTile lt = locate_tile<U>(offsets, tile_first, large_ord, nseg, t, tile);
+  for (uint32_t i = threadIdx.x; i < lt.count; i += kHistThreads) {
+    const U k = apply_xform<U>(keys[lt.base + i], xf);
+#pragma unroll
+    for (int p = 0; p < PASSES; ++p) atomicAdd(&sh[p][uint32_t(k >> (p * kRadixBits)) & (kRadix - 1)], 1u);
+  }
+  __syncthreads();
+  uint32_t *dst = seg_hist + size_t(lt.ord) * PASSES * kRadix;
+  for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) {
+    const uint32_t c = (&sh[0][0])[i];
+    if (c) atomicAdd(&dst[i], c);
+  }
+}
+
+// Per large segment and pass: exclusive scan of the 256 digit counts, plus the
+// segment's first element, in place.
+template <int PASSES>
+__global__ void __launch_bounds__(kRadix)
+segsort_starts_kernel(const unsigned long long *__restrict__ offsets, const uint32_t *__restrict__ seg_of_large,
+                      const uint32_t *__restrict__ totals, uint32_t *__restrict__ seg_hist) {
+  __shared__ uint32_t warp_sum[kRadix / kWarp];
+  const uint32_t k = blockIdx.x;
+  if (k >= totals[1]) return;
+  const uint32_t seg_begin = uint32_t(offsets[seg_of_large[k]]);
+  const unsigned d = threadIdx.x, lane = lane_id(), w = d / kWarp;
+  for (int p = 0; p < PASSES; ++p) {
+    uint32_t *h = seg_hist + (size_t(k) * PASSES + p) * kRadix;
+    const uint32_t c = h[d];
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < kWarp; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (int(lane) >= o) incl += t;
+    }
+    if (lane == kWarp - 1) warp_sum[w] = incl;
+    __syncthreads();
+    uint32_t before = 0;
+    for (unsigned j = 0; j < w; ++j) before += warp_sum[j];
+    h[d] = seg_begin + before + incl - c;
+    __syncthreads();
+  }
+}
+
+template <class U, int VB>
+__global__ void __launch_bounds__(kSortThreads)
+segsort_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
+                        typename value_type_of<VB>::type *__restrict__ vals_main,
+                        typename value_type_of<VB>::type *__restrict__ vals_alt, uint32_t n,
+                        const unsigned long long *__restrict__ offsets, uint32_t nseg,
+                        const uint32_t *__restrict__ tile_first, const uint32_t *__restrict__ large_ord,
+                        const uint32_t *__restrict__ totals, int pass, int passes, const KeyXform<U> xf,
+                        const uint32_t *__restrict__ digit_start, uint32_t *__restrict__ status,
+                        uint32_t *__restrict__ tile_counter, uint32_t *err) {
+  constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
+  __shared__ uint32_t s_tile;
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+  __syncthreads();
+  const uint32_t t = s_tile;
+  if (t >= totals[0]) return;
+  const LargeTile lt = locate_tile<U>(offsets, tile_first, large_ord, nseg, t, TILE);
+  const bool from_alt = (pass & 1) != 0;
+  onesweep_tile<U, VB>(from_alt ? keys_alt : keys_main, from_alt ? keys_main : keys_alt,
+                       from_alt ? vals_alt : vals_main, from_alt ? vals_main : vals_alt, lt.base, lt.count, t,
+                       lt.first_tile, digit_start + (size_t(lt.ord) * passes + pass) * kRadix, n,
+                       pass * kRadixBits, xf, status, err);
+}
+
+// Odd pass counts leave large segments in the temporary buffers.
+template <class U, int VB>
+__global__ void segsort_copyback_kernel(U *__restrict__ keys_main, const U *__restrict__ keys_alt,
+                                        typename value_type_of<VB>::type *__restrict__ vals_main,
+                                        const typename value_type_of<VB>::type *__restrict__ vals_alt,
+                                        const unsigned long long *__restrict__ offsets, uint32_t nseg,
+                                        const uint32_t *__restrict__ tile_first,
+                                        const uint32_t *__restrict__ large_ord,
+                                        const uint32_t *__restrict__ totals) {
+  constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
+  const uint32_t t = blockIdx.x;
+  if (t >= totals[0]) return;
+  const LargeTile lt = locate_tile<U>(offsets, tile_first, large_ord, nseg, t, TILE);
+  for (uint32_t i = threadIdx.x; i < lt.count; i += blockDim.x) {
+    keys_main[lt.base + i] = keys_alt[lt.base + i];
+    if (VB) vals_main[lt.base + i] = vals_alt[lt.base + i];
+  }
+}
+
+// ---- small segments: whole-segment sort in shared memory -------------------
+template <class U, int VB>
+__global__ void __launch_bounds__(kSortThreads)
+segsort_small_kernel(U *__restrict__ keys, typename value_type_of<VB>::type *__restrict__ vals,
+                     const unsigned long long *__restrict__ offsets, uint32_t nseg, int passes,
+                     const KeyXform<U> xf, uint32_t *__restrict__ seg_counter) {
+  typedef typename value_type_of<VB>::type VT;
+  typedef SmallCap<U, VB> C;
+  constexpr int CAP = C::value;
+  constexpr int IPT = C::IPT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t *wcnt = reinterpret_cast<uint32_t *>(smem_raw);
+  U *kbuf = reinterpret_cast<U *>(smem_raw + size_t(kSortWarps) * kRadix * 4);  // [2][CAP]
+  VT *vbuf = reinterpret_cast<VT *>(smem_raw + size_t(kSortWarps) * kRadix * 4 + 2 * size_t(CAP) * sizeof(U));
+  __shared__ uint32_t s_start[kRadix];
+  __shared__ uint32_t s_warp_sum[kSortWarps];
+  __shared__ uint32_t s_seg;
+  __shared__ int s_skip;
+  const unsigned tid = threadIdx.x, lane = lane_id(), warp = tid / kWarp;
+  const unsigned lt_mask = lanemask_lt();
+  while (true) {
+    if (tid == 0) s_seg = atomicAdd(seg_counter, 1u);
+    __syncthreads();
+    const uint32_t seg = s_seg;
+    if (seg >= nseg) break;
+    const unsigned long long b = offsets[seg];
+    const uint32_t m = uint32_t(offsets[seg + 1] - b);
+    if (m < 2 || m > uint32_t(CAP)) {
+      __syncthreads();
+      continue;
+    }
+    int cur = 0;
+    for (uint32_t i = tid; i < m; i += kSortThreads) {
+      kbuf[i] = keys[b + i];
+      if (VB) vbuf[i] = vals[b + i];
+    }
+    for (int p = 0; p < passes; ++p) {
+      U *ka = kbuf + size_t(cur) * CAP;
+      U *kb = kbuf + size_t(cur ^ 1) * CAP;
+      VT *va = vbuf + size_t(cur) * CAP;
+      VT *vb = vbuf + size_t(cur ^ 1) * CAP;
+      for (int i = lane; i < kRadix; i += kWarp) wcnt[warp * kRadix + i] = 0;
+      __syncthreads();
+      uint32_t dr[IPT];
+      const uint32_t warp_first = warp * (kWarp * IPT);
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) {
+        const uint32_t e = warp_first + i * kWarp + lane;
+        const bool valid = e < m;
+        const uint32_t d = valid ? (uint32_t(apply_xform<U>(ka[e], xf) >> (p * kRadixBits)) & (kRadix - 1)) : 0u;
+        unsigned grp = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+        for (int bit = 0; bit < kRadixBits; ++bit) {
+          const bool on = (d >> bit) & 1u;
+          const unsigned v = __ballot_sync(0xffffffffu, on);
+          grp &= on ? v : ~v;
+        }
+        const int leader = __ffs(grp) - 1;
+        uint32_t old = 0;
+        if (valid && int(lane) == leader) {
+          old = wcnt[warp * kRadix + d];
+          wcnt[warp * kRadix + d] = old + __popc(grp);
+        }
+        old = __shfl_sync(0xffffffffu, old, valid ? leader : int(lane));
+        dr[i] = valid ? (d | ((old + __popc(grp & lt_mask)) << 8)) : 0x80000000u;
+        __syncwarp();
+      }
+      __syncthreads();
+      // thread tid owns digit tid: prefix over warps, then over digits
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < kSortWarps; ++w) {
+        const uint32_t c = wcnt[w * kRadix + tid];
+        wcnt[w * kRadix + tid] = run;
+        run += c;
+      }
+      uint32_t incl = run;
+#pragma unroll
+      for (int o = 1; o < kWarp; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (int(lane) >= o) incl += t;
+      }
+      if (lane == kWarp - 1) s_warp_sum[warp] = incl;
+      if (tid == 0) s_skip = 0;
+      __syncthreads();
+      uint32_t before = 0;
+      for (unsigned j = 0; j < warp; ++j) before += s_warp_sum[j];
+      s_start[tid] = before + incl - run;
+      if (run == m) s_skip = 1;  // one digit holds the whole segment: identity pass
+      __syncthreads();
+      if (!s_skip) {
+#pragma unroll
+        for (int i = 0; i < IPT; ++i) {
+          if (!(dr[i] & 0x80000000u)) {
+            const uint32_t d = dr[i] & 0xffu;
+            const uint32_t pos = s_start[d] + wcnt[warp * kRadix + d] + (dr[i] >> 8);
+            const uint32_t e = warp_first + i * kWarp + lane;
+            kb[pos] = ka[e];
+            if (VB) vb[pos] = va[e];
+          }
+        }
+        cur ^= 1;
+      }
+      __syncthreads();
+    }
+    const U *kf = kbuf + size_t(cur) * CAP;
+    const VT *vf = vbuf + size_t(cur) * CAP;
+    for (uint32_t i = tid; i < m; i += kSortThreads) {
+      keys[b + i] = kf[i];
+      if (VB) vals[b + i] = vf[i];
+    }
+    __syncthreads();
+  }
+}
+
+// ---- host ------------------------------------------------------------------
+struct SegLayout {
+  size_t alt_keys, alt_vals, tile_first, large_ord, seg_of_large, totals, counters, seg_hist, status, total;
+  size_t zero_begin, zero_bytes;
+  uint32_t max_tiles, max_large;
+};
+
+template <class U, int VB>
+SegLayout seg_layout(size_t n, size_t nseg) {
+  typedef typename value_type_of<VB>::type VT;
+  constexpr int PASSES = int(sizeof(U));
+  constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
+  SegLayout L;
+  const size_t cap = SmallCap<U, VB>::value;
+  L.max_large = uint32_t(std::min<size_t>(nseg, n / (cap + 1) + 1));
+  L.max_tiles = uint32_t(n / TILE + L.max_large + 1);
+  size_t off = 0;
+  L.alt_keys = off;
+  off += align256(n * sizeof(U));
+  L.alt_vals = off;
+  off += VB ? align256(n * sizeof(VT)) : 0;
+  L.tile_first = off;
+  off += align256((nseg + 1) * 4);
+  L.large_ord = off;
+  off += align256(nseg * 4);
+  L.seg_of_large = off;
+  off += align256(nseg * 4);
+  L.totals = off;
+  off += 256;
+  L.counters = off;  // small-segment ticket + one ticket per pass
+  off += 256;
+  L.seg_hist = off;
+  off += align256(size_t(L.max_large) * PASSES * kRadix * 4);
+  L.status = off;
+  off += align256(size_t(PASSES) * L.max_tiles * kRadix * 4);
+  L.total = off;
+  L.zero_begin = L.counters;
+  L.zero_bytes = off - L.counters;
+  return L;
+}
+
+template <class U, int VB>
+bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const unsigned long long *offsets,
+                     size_t nseg, int kind, int desc, void *temp, size_t *temp_bytes) {
+  typedef typename value_type_of<VB>::type VT;
+  constexpr int PASSES = int(sizeof(U));
+  constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
+  BCX_CHECK(n < (size_t(1) << 31), BCX_INVALID_VALUE, "segmented sort: n must be below 2^31");
+  BCX_CHECK(nseg < (size_t(1) << 31), BCX_INVALID_VALUE, "segmented sort: too many segments");
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
+  const SegLayout L = seg_layout<U, VB>(n, nseg);
+  TempStorage ts;
+  bool query = false;
+  rc = ts.acquire(temp, temp_bytes, L.total, s, &query);
+  if (rc || query) return rc;
+  char *base = static_cast<char *>(ts.ptr());
+  U *k_main = static_cast<U *>(keys);
+  U *k_alt = reinterpret_cast<U *>(base + L.alt_keys);
+  VT *v_main = static_cast<VT *>(values);
+  VT *v_alt = VB ? reinterpret_cast<VT *>(base + L.alt_vals) : nullptr;
+  uint32_t *tile_first = reinterpret_cast<uint32_t *>(base + L.tile_first);
+  uint32_t *large_ord = reinterpret_cast<uint32_t *>(base + L.large_ord);
+  uint32_t *seg_of_large = reinterpret_cast<uint32_t *>(base + L.seg_of_large);
+  uint32_t *totals = reinterpret_cast<uint32_t *>(base + L.totals);
+  uint32_t *counters = reinterpret_cast<uint32_t *>(base + L.counters);
+  uint32_t *seg_hist = reinterpret_cast<uint32_t *>(base + L.seg_hist);
+  uint32_t *status = reinterpret_cast<uint32_t *>(base + L.status);
+  const KeyXform<U> xf = make_xform<U>(kind, desc);
+  BCX_CUDA(cudaMemsetAsync(base + L.zero_begin, 0, L.zero_bytes, s));
+  {
+    KernelScope ks("segsort_plan", s);
+    segsort_plan_kernel<<<1, kPlanThreads, 0, s>>>(offsets, uint32_t(nseg), uint32_t(SmallCap<U, VB>::value),
+                                                   TILE, tile_first, large_ord, seg_of_large, totals);
+    rc = launch_status("segsort_plan");
+    if (rc) return rc;
+  }
+  {
+    constexpr size_t smem = SmallCap<U, VB>::kBytes;
+    static bool attr = false;
+    if (!attr) {
+      BCX_CUDA(cudaFuncSetAttribute(segsort_small_kernel<U, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(smem)));
+      attr = true;
+    }
+    size_t blocks = size_t(ds->sm_count) * 4;
+    if (blocks > nseg) blocks = nseg;
+    KernelScope ks("segsort_small", s);
+    segsort_small_kernel<U, VB><<<unsigned(blocks), kSortThreads, smem, s>>>(k_main, v_main, offsets,
+                                                                              uint32_t(nseg), PASSES, xf, counters);
+    rc = launch_status("segsort_small");
+    if (rc) return rc;
+  }
+  {
+    KernelScope ks("segsort_hist", s);
+    segsort_hist_kernel<U, PASSES><<<L.max_tiles, kHistThreads, 0, s>>>(
+        k_main, offsets, uint32_t(nseg), tile_first, large_ord, totals, TILE, xf, seg_hist);
+    rc = launch_status("segsort_hist");
+    if (rc) return rc;
+  }
+  {
+    KernelScope ks("segsort_starts", s);
+    segsort_starts_kernel<PASSES><<<L.max_large, kRadix, 0, s>>>(offsets, seg_of_large, totals, seg_hist);
+    rc = launch_status("segsort_starts");
+    if (rc) return rc;
+  }
+  constexpr size_t smem = OnesweepSmem<U, VB>::kBytes;
+  static bool attr2 = false;
+  if (!attr2) {
+    BCX_CUDA(cudaFuncSetAttribute(segsort_onesweep_kernel<U, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(smem)));
+    attr2 = true;
+  }
+  for (int p = 0; p < PASSES; ++p) {
+    KernelScope ks("segsort_onesweep", s);
+    segsort_onesweep_kernel<U, VB><<<L.max_tiles, kSortThreads, smem, s>>>(
+        k_main, k_alt, v_main, v_alt, uint32_t(n), offsets, uint32_t(nseg), tile_first, large_ord, totals, p,
+        PASSES, xf, seg_hist, status + size_t(p) * L.max_tiles * kRadix, counters + 1 + p, ds->err_word);
+    rc = launch_status("segsort_onesweep");
+    if (rc) return rc;
+  }
+  if (PASSES & 1) {
+    KernelScope ks("segsort_copyback", s);
+    segsort_copyback_kernel<U, VB><<<L.max_tiles, 256, 0, s>>>(k_main, k_alt, v_main, v_alt, offsets,
+                                                               uint32_t(nseg), tile_first, large_ord, totals);
+    rc = launch_status("segsort_copyback");
+  }
+  return rc;
+}
+
+template <class U>
+bcx_status segsort_vb(cudaStream_t s, size_t vb, void *k, void *v, size_t n, const unsigned long long *offs,
+                      size_t nseg, int kind, int desc, void *temp, size_t *tb) {
+  switch (vb) {
+    case 0: return segsort_t<U, 0>(s, k, v, n, offs, nseg, kind, desc, temp, tb);
+    case 1: return segsort_t<U, 1>(s, k, v, n, offs, nseg, kind, desc, temp, tb);
+    case 2: return segsort_t<U, 2>(s, k, v, n, offs, nseg, kind, desc, temp, tb);
+    case 4: return segsort_t<U, 4>(s, k, v, n, offs, nseg, kind, desc, temp, tb);
+    case 8: return segsort_t<U, 8>(s, k, v, n, offs, nseg, kind, desc, temp, tb);
+    case 16: return segsort_t<U, 16>(s, k, v, n, offs, nseg, kind, desc, temp, tb);
+  }
+  set_error("segmented sort: value size %zu not in {1,2,4,8,16}", vb);
+  return BCX_INVALID_VALUE;
+}
+
+}  // namespace
+}  // namespace bcx
+
+using namespace bcx;
+
+extern "C" bcx_status bcx_segmented_sort_pairs(bcx_stream stream, bcx_dtype key_type, size_t value_bytes,
+                                               void *keys, void *values, size_t n, const uint64_t *offsets,
+                                               size_t nseg, int descending, void *temp, size_t *temp_bytes) {
+  clear_error();
+  BCX_CHECK(dtype_valid(key_type), BCX_INVALID_VALUE, "invalid key dtype %d", int(key_type));
+  if (n == 0 || nseg == 0) {
+    if (temp == nullptr && temp_bytes != nullptr) *temp_bytes = 0;
+    return BCX_SUCCESS;
+  }
+  BCX_CHECK(keys && offsets, BCX_INVALID_VALUE, "NULL argument");
+  BCX_CHECK(value_bytes == 0 || values, BCX_INVALID_VALUE, "values is NULL");
+  const int kind = (key_type == BCX_FLOAT || key_type == BCX_DOUBLE)
+                       ? 2
+                       : ((key_type == BCX_CHAR || key_type == BCX_SHORT || key_type == BCX_INT || key_type == BCX_LONG)
+                              ? 1
+                              : 0);
+  const auto *offs = reinterpret_cast<const unsigned long long *>(offsets);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int desc = descending ? 1 : 0;
+  switch (dtype_size(key_type)) {
+    case 1: return segsort_vb<uint8_t>(s, value_bytes, keys, values, n, offs, nseg, kind, desc, temp, temp_bytes);
+    case 2: return segsort_vb<uint16_t>(s, value_bytes, keys, values, n, offs, nseg, kind, desc, temp, temp_bytes);
+    case 4: return segsort_vb<uint32_t>(s, value_bytes, keys, values, n, offs, nseg, kind, desc, temp, temp_bytes);
+    case 8:
+      return segsort_vb<unsigned long long>(s, value_bytes, keys, values, n, offs, nseg, kind, desc, temp,
+                                            temp_bytes);
+  }
+  return BCX_INVALID_VALUE;
+}

@@ -232,6 +232,17 @@ bcx_status bcx_segmented_reduce(bcx_stream stream, bcx_dtype type, bcx_op op, co
                                 const uint64_t *offsets, size_t nseg, const void *init, void *out,
                                 int compensated, void *temp, size_t *temp_bytes);
 
+/* Segmented sort / sort_by_key: every segment [offsets[s], offsets[s+1]) is
+ * sorted independently and stably in the order of bcx_radix_sort_pairs
+ * (value_bytes = 0 sorts keys only).  Replaces one sort_by_key call per
+ * segment (sort_by_key.hpp:33-163).  Small segments are sorted in shared
+ * memory by one block each, large ones by segment-confined onesweep passes;
+ * all work is asynchronous on `stream` and reads nothing back, so the call
+ * can be captured in a CUDA graph.  n < 2^31. */
+bcx_status bcx_segmented_sort_pairs(bcx_stream stream, bcx_dtype key_type, size_t value_bytes,
+                                    void *keys, void *values, size_t n, const uint64_t *offsets,
+                                    size_t nseg, int descending, void *temp, size_t *temp_bytes);
+
 /* ---- run-time compiled kernels ------------------------------------------
  * Replaces clBuildProgram + program_cache (utility/program_cache.hpp:52-168,
  * program.hpp:638-692) and the offline binary cache (program.hpp:656-690):

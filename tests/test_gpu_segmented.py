@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 NP = {"int": np.int32, "uint": np.uint32, "long": np.int64, "ulong": np.uint64, "float": np.float32,
       "double": np.float64}
 TORCH_NP = {"int": np.int32, "uint": np.int32, "long": np.int64, "ulong": np.int64, "float": np.float32,
-            "double": np.float64}
+            "double": np.float64, "uchar": np.uint8}
 
 
 def log_uniform_offsets(rng, nseg, lo, hi, empty_frac=0.0):
@@ -100,3 +100,52 @@ def test_segmented_reduce_matches_per_segment(cuda, dtype, op):
             assert got[s] == NP[dtype](oracle.sum_f64(x[a:b], dtype, init=float(init[0]))), s
         else:
             assert got[s] == ref, (s, got[s], ref)
+
+
+def run_seg_sort(torch, keys, vals, kt, offsets, descending=False):
+    from compute_gb300 import _lib
+    lib = _lib.lib()
+    dk = torch.from_numpy(keys.view(TORCH_NP.get(kt, keys.dtype)).copy()).cuda()
+    dv = torch.from_numpy(vals.copy()).cuda() if vals is not None else None
+    offs = torch.from_numpy(offsets.view(np.int64).copy()).cuda()
+    vb = vals.dtype.itemsize if vals is not None else 0
+    rc = lib.bcx_segmented_sort_pairs(torch.cuda.current_stream().cuda_stream, _lib.DTYPES[kt], vb, dk.data_ptr(),
+                                      dv.data_ptr() if dv is not None else None, keys.size, offs.data_ptr(),
+                                      offsets.size - 1, int(descending), None, None)
+    assert rc == 0, lib.bcx_last_error_string()
+    assert lib.bcx_device_error_check(torch.cuda.current_stream().cuda_stream) == 0
+    return dk.cpu().numpy().view(keys.dtype), (dv.cpu().numpy() if dv is not None else None)
+
+
+@pytest.mark.parametrize("kt", ["uint", "int", "float", "ulong"])
+@pytest.mark.parametrize("descending", [False, True])
+def test_segmented_sort_pairs_matches_per_segment(cuda, kt, descending):
+    rng = np.random.default_rng(11)
+    # log-uniform sizes from 1 to 3e5: both the shared-memory and the onesweep paths
+    offsets = log_uniform_offsets(rng, 300, 1, 300_000, empty_frac=0.03)
+    n = int(offsets[-1])
+    if kt == "float":
+        keys = (rng.standard_normal(n) * 100).astype(np.float32)
+        keys[rng.integers(0, n, size=n // 50)] = -0.0
+    elif kt == "ulong":
+        keys = rng.integers(0, 2**63, size=n, dtype=np.int64).astype(np.uint64) * 2
+    else:
+        keys = rng.integers(0, 1 << 20, size=n).astype(NP[kt])  # many equal keys: stability matters
+    vals = np.arange(n, dtype=np.uint32)
+    gk, gv = run_seg_sort(cuda, keys, vals, kt, offsets, descending)
+    for s in range(offsets.size - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        rk, rv = oracle.radix_sort(keys[a:b], kt, values=vals[a:b], descending=descending)
+        np.testing.assert_array_equal(gk[a:b].view(np.uint8), rk.view(np.uint8), err_msg=f"keys seg {s} [{a},{b})")
+        np.testing.assert_array_equal(gv[a:b], rv, err_msg=f"values seg {s} [{a},{b})")
+
+
+def test_segmented_sort_keys_only_and_8bit(cuda):
+    rng = np.random.default_rng(12)
+    offsets = log_uniform_offsets(rng, 80, 1, 50_000)
+    n = int(offsets[-1])
+    keys = rng.integers(0, 256, size=n).astype(np.uint8)
+    gk, _ = run_seg_sort(cuda, keys, None, "uchar", offsets)
+    for s in range(offsets.size - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        np.testing.assert_array_equal(gk[a:b], np.sort(keys[a:b], kind="stable"))
