@@ -69,6 +69,14 @@ SIGNATURES = {
     "bcx_segmented_scan": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp, _sz, _i, _vp, _szp]),
     "bcx_segmented_reduce": (_i, [_vp, _i, _i, _vp, _vp, _sz, _vp, _vp, _i, _vp, _szp]),
     "bcx_segmented_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _vp, _sz, _i, _vp, _szp]),
+    "bcx_server_create": (_i, [C.POINTER(_vp), _i, _sz]),
+    "bcx_server_configure": (_i, [_vp, _sz, _sz, _sz]),
+    "bcx_server_submit": (_i, [_vp, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "bcx_server_wait": (_i, [_vp, C.c_uint64, C.POINTER(C.c_double)]),
+    "bcx_server_drain": (_i, [_vp]),
+    "bcx_server_stats": (_i, [_vp, C.c_void_p]),
+    "bcx_server_reset_stats": (_i, [_vp]),
+    "bcx_server_destroy": (_i, [_vp]),
     "bcx_jit_get_kernel": (_i, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(_vp)]),
     "bcx_jit_launch": (_i, [_vp, C.c_uint, C.c_uint, _sz, _vp, C.POINTER(_vp)]),
     "bcx_jit_build_log": (_i, [C.c_char_p, _sz, _szp]),
@@ -79,6 +87,20 @@ SIGNATURES = {
     "bcx_profile_reset": (_i, []),
     "bcx_profile_read": (_i, [C.c_char_p, _sz, C.POINTER(C.c_uint64), C.POINTER(C.c_double), _sz, _szp]),
 }
+
+
+class Request(C.Structure):
+    """bcx_request (include/bcx.h)."""
+    _fields_ = [("kind", C.c_int), ("dtype", C.c_int), ("value_bytes", C.c_size_t), ("n", C.c_size_t),
+                ("flags", C.c_int), ("keys", C.c_void_p), ("values", C.c_void_p), ("out", C.c_void_p),
+                ("out_values", C.c_void_p)]
+
+
+class ServerStats(C.Structure):
+    """bcx_server_stats_t (include/bcx.h)."""
+    _fields_ = [("completed", C.c_uint64), ("batches", C.c_uint64), ("batched_requests", C.c_uint64),
+                ("pending", C.c_uint64), ("used_bytes", C.c_size_t), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("max_ms", C.c_double)]
 
 
 class BcxError(RuntimeError):

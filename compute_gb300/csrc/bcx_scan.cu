@@ -382,7 +382,7 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   }
 }
 
-template <class T> struct scan_vectors_per_thread { static constexpr int value = 4; };
+template <class T> struct scan_vectors_per_thread { static constexpr int value = 8; };
 
 template <class T, class P>
 bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const void *in, void *out,
@@ -516,6 +516,7 @@ namespace bcx {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
+constexpr int kNoAllocVectorsPerThread = 4;
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[kNoAllocScratchBytes];
 
 // Device address of the scratch array on the current device.  In host code
@@ -547,7 +548,9 @@ bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, c
   typedef typename P::Carry Carry;
   typedef TileStatus<Carry> Status;
   constexpr int N = 16 / sizeof(T);
-  constexpr int V = scan_vectors_per_thread<T>::value;
+  // Fixed tile shape, so the size limit of the fixed scratch array does not
+  // move when the allocating scan is retuned.
+  constexpr int V = kNoAllocVectorsPerThread;
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;

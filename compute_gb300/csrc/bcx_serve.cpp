@@ -1,0 +1,457 @@
+// bcx_serve.cpp -- continuous-batching request server for sort_by_key,
+// exclusive_scan and reduce.
+//
+// The reference has no serving layer: a caller issues one algorithm call at a
+// time on a queue and blocks on each result (e.g. reduce into a host pointer,
+// reduce.hpp:225).  This server accepts requests from any thread while
+// earlier ones are on the GPU:
+//   * a scheduler thread admits requests in arrival order whenever a slot
+//     (a CUDA stream) is free and the device-memory budget covers the
+//     request's buffers and temporaries;
+//   * small requests that wait together with the same (kind, dtype, value
+//     size) are packed into one batch and run as ONE segmented launch
+//     (bcx_segmented_sort_pairs / bcx_segmented_scan / bcx_segmented_reduce);
+//     large requests run alone with the plain kernels;
+//   * each batch copies its inputs in, computes and copies results out on its
+//     slot stream, so copies and kernels of different batches overlap;
+//   * a host callback on the slot stream stamps the completion time of every
+//     request in the batch and returns its memory to the budget.
+// Buffers may be host memory (copied in and out on the slot stream) or
+// device-resident (copied device to device into the batch and back; a lone
+// request still computes in its own batch buffer so inputs stay untouched).
+// Integer results are identical alone and batched; float scan/reduce use the
+// compensated kernels in both cases (same tolerance, possibly different
+// association).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "bcx.h"
+#include "bcx_internal.h"
+
+namespace bcx {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  uint64_t ticket;
+  bcx_request r;
+  Clock::time_point submitted;
+  Clock::time_point finished;
+  std::atomic<int> done{0};
+  bcx_status status = BCX_SUCCESS;
+};
+
+struct Batch;
+
+struct Slot {
+  cudaStream_t stream = nullptr;
+  bool busy = false;
+};
+
+struct Batch {
+  struct bcx_server *server = nullptr;
+  int slot = -1;
+  std::vector<std::shared_ptr<Request>> reqs;
+  size_t bytes = 0;  // budget charged
+  void *dev = nullptr;  // one device allocation for the whole batch
+};
+
+size_t elem_size(bcx_dtype t) { return dtype_size(t); }
+
+}  // namespace
+}  // namespace bcx
+
+struct bcx_server {
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<std::shared_ptr<bcx::Request>> pending;
+  std::map<uint64_t, std::shared_ptr<bcx::Request>> all;
+  std::vector<bcx::Slot> slots;
+  size_t budget = 0, used = 0;
+  size_t small_limit = 1 << 18;     // requests up to this many elements may be batched
+  size_t batch_elems = 1 << 24;     // elements per batch
+  size_t batch_count = 4096;        // requests per batch
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  std::thread scheduler;
+  int device = 0;
+  // statistics
+  uint64_t completed = 0, batches = 0, batched_requests = 0;
+  std::vector<double> latencies_ms;
+};
+
+namespace bcx {
+namespace {
+
+// Device bytes a request needs (inputs/outputs plus its temporaries, for a
+// batch of one).
+size_t request_bytes(const bcx_request &r) {
+  const size_t es = elem_size(r.dtype);
+  switch (r.kind) {
+    case BCX_REQ_SORT_PAIRS: return align256(r.n * es) + align256(r.n * r.value_bytes);
+    case BCX_REQ_EXCLUSIVE_SCAN: return 2 * align256(r.n * es);
+    case BCX_REQ_REDUCE: return align256(r.n * es) + 256;
+  }
+  return 0;
+}
+
+void CUDART_CB on_batch_done(void *p) {
+  Batch *b = static_cast<Batch *>(p);
+  const auto now = Clock::now();
+  bcx_server *srv = b->server;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (auto &r : b->reqs) {
+      r->finished = now;
+      r->done.store(1);
+      srv->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->submitted).count());
+    }
+    srv->completed += b->reqs.size();
+    srv->used -= b->bytes;
+    srv->slots[b->slot].busy = false;
+  }
+  srv->cv.notify_all();
+  delete b;
+}
+
+// Enqueue one batch on its slot stream.  Called with the server lock held
+// (only enqueues asynchronous work).
+bcx_status launch_batch(bcx_server *srv, Batch *b, size_t temp_bytes) {
+  cudaStream_t s = srv->slots[b->slot].stream;
+  const bcx_request &r0 = b->reqs[0]->r;
+  const size_t es = elem_size(r0.dtype);
+  const size_t k = b->reqs.size();
+  size_t n = 0;
+  for (auto &r : b->reqs) n += r->r.n;
+  // Layout of the batch allocation: keys/input | values or output | offsets | temp
+  const size_t a_keys = 0;
+  const size_t a_second = align256(n * es);
+  const size_t second_bytes = r0.kind == BCX_REQ_SORT_PAIRS ? n * r0.value_bytes
+                              : r0.kind == BCX_REQ_EXCLUSIVE_SCAN ? n * es
+                                                                   : k * es;
+  const size_t a_offs = a_second + align256(second_bytes);
+  const size_t a_temp = a_offs + align256((k + 1) * sizeof(uint64_t));
+  const size_t total = a_temp + temp_bytes;
+  BCX_CUDA(cudaMallocAsync(&b->dev, total, s));
+  char *base = static_cast<char *>(b->dev);
+  // inputs
+  size_t off = 0;
+  std::vector<uint64_t> offsets(k + 1, 0);
+  for (size_t i = 0; i < k; ++i) {
+    const bcx_request &r = b->reqs[i]->r;
+    offsets[i] = off;
+    if (r.n) {
+      BCX_CUDA(cudaMemcpyAsync(base + a_keys + off * es, r.keys, r.n * es, cudaMemcpyDefault, s));
+      if (r.kind == BCX_REQ_SORT_PAIRS && r.value_bytes)
+        BCX_CUDA(cudaMemcpyAsync(base + a_second + off * r.value_bytes, r.values, r.n * r.value_bytes,
+                                 cudaMemcpyDefault, s));
+    }
+    off += r.n;
+  }
+  offsets[k] = off;
+  // The offsets come from a host vector that dies with this function: stage
+  // them through pageable-memory semantics (cudaMemcpyAsync from pageable
+  // memory returns once the source has been consumed).
+  BCX_CUDA(cudaMemcpyAsync(base + a_offs, offsets.data(), (k + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  const uint64_t *d_offs = reinterpret_cast<const uint64_t *>(base + a_offs);
+  // A NULL temp with a size pointer would be a size query: pass no pointer
+  // when the call needs no temporary storage.
+  void *tmp = temp_bytes ? base + a_temp : nullptr;
+  size_t tb_val = temp_bytes;
+  size_t *tbp = temp_bytes ? &tb_val : nullptr;
+  bcx_status rc = BCX_SUCCESS;
+  const int comp = (r0.dtype == BCX_FLOAT || r0.dtype == BCX_DOUBLE) ? 1 : 0;
+  if (r0.kind == BCX_REQ_SORT_PAIRS) {
+    if (k == 1)
+      rc = r0.value_bytes ? bcx_sort_pairs(s, r0.dtype, r0.value_bytes, base + a_keys, base + a_second, n, 0, tmp, tbp)
+                          : bcx_sort_keys(s, r0.dtype, base + a_keys, n, 0, tmp, tbp);
+    else
+      rc = bcx_segmented_sort_pairs(s, r0.dtype, r0.value_bytes, base + a_keys, base + a_second, n, d_offs, k, 0,
+                                    tmp, tbp);
+  } else if (r0.kind == BCX_REQ_EXCLUSIVE_SCAN) {
+    unsigned char zero[8] = {0};
+    if (k == 1)
+      rc = bcx_scan(s, r0.dtype, BCX_PLUS, 1, zero, base + a_keys, base + a_second, n, comp, tmp, tbp);
+    else
+      rc = bcx_segmented_scan(s, r0.dtype, BCX_PLUS, 1, zero, base + a_keys, base + a_second, n, d_offs, k, comp,
+                              tmp, tbp);
+  } else {
+    unsigned char zero[8] = {0};
+    if (k == 1)
+      rc = bcx_reduce(s, r0.dtype, BCX_PLUS, base + a_keys, n, base + a_second, comp, tmp, tbp);
+    else
+      rc = bcx_segmented_reduce(s, r0.dtype, BCX_PLUS, base + a_keys, d_offs, k, zero, base + a_second, comp, tmp,
+                                tbp);
+  }
+  if (rc) {
+    for (auto &r : b->reqs) r->status = rc;
+  }
+  // outputs
+  off = 0;
+  for (size_t i = 0; i < k; ++i) {
+    const bcx_request &r = b->reqs[i]->r;
+    if (r.kind == BCX_REQ_SORT_PAIRS) {
+      if (r.n) {
+        BCX_CUDA(cudaMemcpyAsync(r.out, base + a_keys + off * es, r.n * es, cudaMemcpyDefault, s));
+        if (r.value_bytes)
+          BCX_CUDA(cudaMemcpyAsync(r.out_values, base + a_second + off * r.value_bytes, r.n * r.value_bytes,
+                                   cudaMemcpyDefault, s));
+      }
+    } else if (r.kind == BCX_REQ_EXCLUSIVE_SCAN) {
+      if (r.n) BCX_CUDA(cudaMemcpyAsync(r.out, base + a_second + off * es, r.n * es, cudaMemcpyDefault, s));
+    } else {
+      BCX_CUDA(cudaMemcpyAsync(r.out, base + a_second + i * es, es, cudaMemcpyDefault, s));
+    }
+    off += r.n;
+  }
+  BCX_CUDA(cudaFreeAsync(b->dev, s));
+  BCX_CUDA(cudaLaunchHostFunc(s, on_batch_done, b));
+  return BCX_SUCCESS;
+}
+
+// Temporary bytes of a batch (query protocol of the underlying call).  The
+// query sees 256-byte aligned stand-in pointers, like the batch allocation's.
+size_t batch_temp(const std::vector<std::shared_ptr<Request>> &reqs, size_t n) {
+  const bcx_request &r0 = reqs[0]->r;
+  const size_t k = reqs.size();
+  size_t tb = 0;
+  unsigned char zero[8] = {0};
+  void *p = reinterpret_cast<void *>(uintptr_t(256));
+  const uint64_t *po = reinterpret_cast<const uint64_t *>(p);
+  bcx_status rc = BCX_SUCCESS;
+  if (r0.kind == BCX_REQ_SORT_PAIRS) {
+    if (k == 1)
+      rc = r0.value_bytes ? bcx_sort_pairs(nullptr, r0.dtype, r0.value_bytes, p, p, n, 0, nullptr, &tb)
+                          : bcx_sort_keys(nullptr, r0.dtype, p, n, 0, nullptr, &tb);
+    else
+      rc = bcx_segmented_sort_pairs(nullptr, r0.dtype, r0.value_bytes, p, p, n, po, k, 0, nullptr, &tb);
+  } else if (r0.kind == BCX_REQ_EXCLUSIVE_SCAN) {
+    const int comp = (r0.dtype == BCX_FLOAT || r0.dtype == BCX_DOUBLE) ? 1 : 0;
+    if (k == 1) rc = bcx_scan(nullptr, r0.dtype, BCX_PLUS, 1, zero, p, p, n, comp, nullptr, &tb);
+    else rc = bcx_segmented_scan(nullptr, r0.dtype, BCX_PLUS, 1, zero, p, p, n, po, k, comp, nullptr, &tb);
+  } else {
+    const int comp = (r0.dtype == BCX_FLOAT || r0.dtype == BCX_DOUBLE) ? 1 : 0;
+    if (k == 1) rc = bcx_reduce(nullptr, r0.dtype, BCX_PLUS, p, n, p, comp, nullptr, &tb);
+    else rc = bcx_segmented_reduce(nullptr, r0.dtype, BCX_PLUS, p, po, k, zero, p, comp, nullptr, &tb);
+  }
+  return rc ? 0 : tb;
+}
+
+bool same_group(const bcx_request &a, const bcx_request &b) {
+  return a.kind == b.kind && a.dtype == b.dtype && a.value_bytes == b.value_bytes;
+}
+
+void scheduler_loop(bcx_server *srv) {
+  cudaSetDevice(srv->device);
+  std::unique_lock<std::mutex> lk(srv->mu);
+  while (true) {
+    srv->cv.wait(lk, [&] {
+      if (srv->stop) return true;
+      if (srv->pending.empty()) return false;
+      for (auto &sl : srv->slots)
+        if (!sl.busy) return true;
+      return false;
+    });
+    if (srv->stop && srv->pending.empty()) break;
+    int slot = -1;
+    for (size_t i = 0; i < srv->slots.size(); ++i)
+      if (!srv->slots[i].busy) {
+        slot = int(i);
+        break;
+      }
+    if (slot < 0 || srv->pending.empty()) continue;
+    // Build a batch around the oldest request.
+    auto first = srv->pending.front();
+    std::vector<std::shared_ptr<Request>> reqs{first};
+    size_t n = first->r.n;
+    if (first->r.n <= srv->small_limit) {
+      for (auto it = srv->pending.begin() + 1; it != srv->pending.end(); ++it) {
+        const auto &q = *it;
+        if (reqs.size() >= srv->batch_count) break;
+        if (!same_group(q->r, first->r) || q->r.n > srv->small_limit) continue;
+        if (n + q->r.n > srv->batch_elems) break;
+        reqs.push_back(q);
+        n += q->r.n;
+      }
+    }
+    size_t bytes = 0;
+    for (auto &r : reqs) bytes += request_bytes(r->r);
+    const size_t temp = batch_temp(reqs, n);
+    bytes += temp + 2 * 256 + align256((reqs.size() + 1) * 8);
+    if (srv->used + bytes > srv->budget && srv->used > 0) {
+      // Not enough memory right now: wait for a completion to free some.
+      srv->cv.wait(lk);
+      continue;
+    }
+    // Admit: remove from pending (preserving the order of the rest).
+    for (auto &r : reqs) {
+      auto it = std::find(srv->pending.begin(), srv->pending.end(), r);
+      if (it != srv->pending.end()) srv->pending.erase(it);
+    }
+    Batch *b = new Batch();
+    b->server = srv;
+    b->slot = slot;
+    b->reqs = reqs;
+    b->bytes = bytes;
+    srv->slots[slot].busy = true;
+    srv->used += bytes;
+    srv->batches += 1;
+    if (reqs.size() > 1) srv->batched_requests += reqs.size();
+    bcx_status rc = launch_batch(srv, b, temp);
+    if (rc) {
+      for (auto &r : reqs) {
+        r->status = rc;
+        r->finished = Clock::now();
+        r->done.store(1);
+      }
+      srv->used -= bytes;
+      srv->slots[slot].busy = false;
+      delete b;
+      srv->cv.notify_all();
+    }
+  }
+}
+
+}  // namespace
+}  // namespace bcx
+
+using namespace bcx;
+
+extern "C" {
+
+bcx_status bcx_server_create(bcx_server **out, int slots, size_t memory_budget_bytes) {
+  clear_error();
+  BCX_CHECK(out && slots > 0 && slots <= 64, BCX_INVALID_VALUE, "bad server arguments");
+  auto *srv = new bcx_server();
+  BCX_CUDA(cudaGetDevice(&srv->device));
+  if (memory_budget_bytes == 0) {
+    size_t free_b = 0, total_b = 0;
+    BCX_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    memory_budget_bytes = free_b / 2;
+  }
+  srv->budget = memory_budget_bytes;
+  srv->slots.resize(size_t(slots));
+  for (auto &sl : srv->slots) BCX_CUDA(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+  srv->scheduler = std::thread(scheduler_loop, srv);
+  *out = srv;
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_server_configure(bcx_server *srv, size_t small_limit, size_t batch_elems, size_t batch_count) {
+  BCX_CHECK(srv, BCX_INVALID_VALUE, "NULL server");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  srv->small_limit = small_limit;
+  if (batch_elems) srv->batch_elems = batch_elems;
+  if (batch_count) srv->batch_count = batch_count;
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_server_submit(bcx_server *srv, const bcx_request *req, uint64_t *ticket) {
+  clear_error();
+  BCX_CHECK(srv && req && ticket, BCX_INVALID_VALUE, "NULL argument");
+  BCX_CHECK(req->kind >= BCX_REQ_SORT_PAIRS && req->kind <= BCX_REQ_REDUCE, BCX_INVALID_VALUE, "bad request kind");
+  BCX_CHECK(dtype_valid(req->dtype), BCX_INVALID_VALUE, "bad dtype");
+  BCX_CHECK(req->n == 0 || req->keys, BCX_INVALID_VALUE, "request without input");
+  BCX_CHECK(req->n == 0 || req->out, BCX_INVALID_VALUE, "request without output");
+  BCX_CHECK(req->kind != BCX_REQ_SORT_PAIRS || req->value_bytes == 0 || (req->values && req->out_values),
+            BCX_INVALID_VALUE, "sort request without values");
+  auto r = std::make_shared<Request>();
+  r->r = *req;
+  r->submitted = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    BCX_CHECK(request_bytes(*req) <= srv->budget, BCX_MEM_ALLOCATION_FAILURE,
+              "request needs more device memory than the server budget");
+    r->ticket = srv->next_ticket++;
+    srv->pending.push_back(r);
+    srv->all[r->ticket] = r;
+    *ticket = r->ticket;
+  }
+  srv->cv.notify_all();
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_server_wait(bcx_server *srv, uint64_t ticket, double *latency_ms) {
+  BCX_CHECK(srv, BCX_INVALID_VALUE, "NULL server");
+  std::shared_ptr<Request> r;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->all.find(ticket);
+    BCX_CHECK(it != srv->all.end(), BCX_INVALID_VALUE, "unknown ticket %llu", (unsigned long long)ticket);
+    r = it->second;
+  }
+  std::unique_lock<std::mutex> lk(srv->mu);
+  srv->cv.wait(lk, [&] { return r->done.load() != 0; });
+  if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->finished - r->submitted).count();
+  srv->all.erase(ticket);
+  if (r->status) set_error("request %llu failed", (unsigned long long)ticket);
+  return r->status;
+}
+
+bcx_status bcx_server_drain(bcx_server *srv) {
+  BCX_CHECK(srv, BCX_INVALID_VALUE, "NULL server");
+  std::unique_lock<std::mutex> lk(srv->mu);
+  srv->cv.wait(lk, [&] {
+    if (!srv->pending.empty()) return false;
+    for (auto &sl : srv->slots)
+      if (sl.busy) return false;
+    return true;
+  });
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_server_stats(bcx_server *srv, bcx_server_stats_t *st) {
+  BCX_CHECK(srv && st, BCX_INVALID_VALUE, "NULL argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  std::memset(st, 0, sizeof(*st));
+  st->completed = srv->completed;
+  st->batches = srv->batches;
+  st->batched_requests = srv->batched_requests;
+  st->pending = srv->pending.size();
+  st->used_bytes = srv->used;
+  std::vector<double> v = srv->latencies_ms;
+  if (!v.empty()) {
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double p) { return v[std::min(v.size() - 1, size_t(p * (v.size() - 1) + 0.5))]; };
+    st->p50_ms = pct(0.50);
+    st->p99_ms = pct(0.99);
+    st->max_ms = v.back();
+  }
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_server_reset_stats(bcx_server *srv) {
+  BCX_CHECK(srv, BCX_INVALID_VALUE, "NULL server");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  srv->completed = srv->batches = srv->batched_requests = 0;
+  srv->latencies_ms.clear();
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_server_destroy(bcx_server *srv) {
+  if (!srv) return BCX_SUCCESS;
+  bcx_server_drain(srv);
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stop = true;
+  }
+  srv->cv.notify_all();
+  if (srv->scheduler.joinable()) srv->scheduler.join();
+  for (auto &sl : srv->slots) cudaStreamDestroy(sl.stream);
+  delete srv;
+  return BCX_SUCCESS;
+}
+
+}  // extern "C"

@@ -243,6 +243,51 @@ bcx_status bcx_segmented_sort_pairs(bcx_stream stream, bcx_dtype key_type, size_
                                     void *keys, void *values, size_t n, const uint64_t *offsets,
                                     size_t nseg, int descending, void *temp, size_t *temp_bytes);
 
+/* ---- request server (continuous batching) --------------------------------
+ * No reference counterpart: the reference serves one blocking call at a time
+ * on a queue.  A server owns `slots` CUDA streams and a device-memory budget
+ * (0 = half of the free memory).  Requests are admitted in arrival order as
+ * slots and memory free up; small waiting requests of the same kind, dtype and
+ * value size are packed into one segmented launch; large ones run alone.
+ * Buffers are host memory (use page-locked memory for copy overlap) or, with
+ * BCX_REQ_DEVICE_RESIDENT, device memory; either way they must stay valid
+ * until bcx_server_wait returns.  Sort requests read keys (and values) and
+ * write the stably sorted pairs to out (and out_values), which may alias the
+ * inputs; scan requests write the exclusive plus-scan of keys to out; reduce
+ * requests write the plus-sum of keys to out[0].  Float scans and sums use the
+ * compensated kernels. */
+typedef struct bcx_server bcx_server;
+typedef enum { BCX_REQ_SORT_PAIRS = 0, BCX_REQ_EXCLUSIVE_SCAN = 1, BCX_REQ_REDUCE = 2 } bcx_req_kind;
+#define BCX_REQ_DEVICE_RESIDENT 1
+typedef struct {
+    int kind;            /* bcx_req_kind */
+    bcx_dtype dtype;     /* key / element type */
+    size_t value_bytes;  /* sort: bytes per value (0 = keys only) */
+    size_t n;            /* elements */
+    int flags;           /* BCX_REQ_DEVICE_RESIDENT: all buffers are device memory */
+    const void *keys;    /* sort keys, scan / reduce input */
+    const void *values;  /* sort values */
+    void *out;           /* sorted keys, scan output (n elements), reduce output (1 element) */
+    void *out_values;    /* sorted values */
+} bcx_request;
+typedef struct {
+    uint64_t completed, batches, batched_requests, pending;
+    size_t used_bytes;
+    double p50_ms, p99_ms, max_ms; /* submit -> results in host memory */
+} bcx_server_stats_t;
+bcx_status bcx_server_create(bcx_server **server, int slots, size_t memory_budget_bytes);
+/* Requests of at most small_limit elements may be batched, up to batch_elems
+ * elements and batch_count requests per batch (0 keeps a value). */
+bcx_status bcx_server_configure(bcx_server *server, size_t small_limit, size_t batch_elems,
+                                size_t batch_count);
+bcx_status bcx_server_submit(bcx_server *server, const bcx_request *request, uint64_t *ticket);
+/* Blocks until the request's results are in host memory. */
+bcx_status bcx_server_wait(bcx_server *server, uint64_t ticket, double *latency_ms);
+bcx_status bcx_server_drain(bcx_server *server);
+bcx_status bcx_server_stats(bcx_server *server, bcx_server_stats_t *stats);
+bcx_status bcx_server_reset_stats(bcx_server *server);
+bcx_status bcx_server_destroy(bcx_server *server);
+
 /* ---- run-time compiled kernels ------------------------------------------
  * Replaces clBuildProgram + program_cache (utility/program_cache.hpp:52-168,
  * program.hpp:638-692) and the offline binary cache (program.hpp:656-690):

@@ -1,0 +1,69 @@
+"""Continuous-batching server: every request's result is the same alone and in
+the mix (integers bit-exact, float scan/sum within the FP64-oracle tolerance),
+and small requests really are batched while larger ones overlap."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+NP = {"int": np.int32, "uint": np.uint32, "float": np.float32, "ulong": np.uint64}
+
+
+def make_requests(rng, count):
+    reqs = []
+    for i in range(count):
+        kind = rng.choice(["sort_by_key", "exclusive_scan", "reduce"], p=[0.5, 0.3, 0.2])
+        dtype = rng.choice(["int", "uint", "float", "ulong"])
+        n = int(np.exp(rng.uniform(np.log(1 << 6), np.log(1 << 20))))
+        if dtype == "float":
+            keys = rng.standard_normal(n).astype(np.float32)
+        elif dtype == "ulong":
+            keys = rng.integers(0, 2**63, size=n, dtype=np.int64).astype(np.uint64)
+        else:
+            keys = rng.integers(-2**31 if dtype == "int" else 0, 2**31, size=n).astype(NP[dtype])
+        reqs.append((kind, dtype, keys))
+    return reqs
+
+
+def test_server_results_match_alone(cuda):
+    from compute_gb300.serve import Server
+    rng = np.random.default_rng(2026)
+    reqs = make_requests(rng, 240)
+    with Server(slots=8) as srv:
+        tickets = []
+        bufs = []
+        for kind, dtype, keys in reqs:
+            k = keys.copy()
+            v = np.arange(k.size, dtype=np.uint32) if kind == "sort_by_key" else None
+            out = None
+            if kind == "exclusive_scan":
+                out = np.empty_like(k)
+            elif kind == "reduce":
+                out = np.zeros(1, dtype=k.dtype)
+            bufs.append((k, v, out))
+            tickets.append(srv.submit(kind, dtype, k, values=v, out=out))
+        lat = [srv.wait(t) for t in tickets]
+        st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["batched_requests"] > 0, st  # small requests were packed into shared launches
+    assert all(x >= 0 for x in lat)
+    for (kind, dtype, keys), (k, v, out) in zip(reqs, bufs):
+        if kind == "sort_by_key":
+            rk, rv = oracle.radix_sort(keys, dtype, values=np.arange(keys.size, dtype=np.uint32))
+            assert np.array_equal(k.view(np.uint8), rk.view(np.uint8))
+            assert np.array_equal(v, rv)
+        elif kind == "exclusive_scan":
+            if dtype == "float":
+                ref = oracle.prefix_f64(keys, "float", exclusive=True)
+                bound = np.concatenate([[0.0], np.cumsum(np.abs(keys.astype(np.float64)))[:-1]]) * 2.0 ** -22 + 1e-30
+                assert (np.abs(out.astype(np.float64) - ref) <= bound).all()
+            else:
+                assert np.array_equal(out, oracle.scan(keys, dtype, exclusive=True))
+        else:
+            if dtype == "float":
+                ref = oracle.sum_f64(keys, "float")
+                assert abs(float(out[0]) - ref) <= float(np.abs(keys.astype(np.float64)).sum()) * 2.0 ** -22 + 1e-30
+            else:
+                assert out[0] == oracle.fold(keys, dtype)
