@@ -1,6 +1,7 @@
 """Python handle on the continuous-batching request server (bcx_server_* in
 include/bcx.h).  Requests reference host buffers (numpy arrays or pinned torch
-tensors) that must stay alive until their ticket has been waited for."""
+tensors) or, with device=True, CUDA tensors; either must stay alive until the
+request's ticket has been waited for."""
 from __future__ import annotations
 
 import ctypes as C

@@ -67,3 +67,34 @@ def test_server_results_match_alone(cuda):
                 assert abs(float(out[0]) - ref) <= float(np.abs(keys.astype(np.float64)).sum()) * 2.0 ** -22 + 1e-30
             else:
                 assert out[0] == oracle.fold(keys, dtype)
+
+
+def test_server_device_resident_out_of_place(cuda):
+    """Device buffers, sorts written out of place: inputs are left untouched and
+    several requests may read the same input buffer."""
+    import torch
+    from compute_gb300.serve import Server
+    rng = np.random.default_rng(7)
+    shared = rng.integers(0, 2**32, size=1 << 16, dtype=np.uint64).astype(np.uint32)
+    dk = torch.from_numpy(shared.view(np.int32)).to("cuda")
+    dv = torch.arange(shared.size, dtype=torch.int32, device="cuda")
+    outs = []
+    with Server(slots=4) as srv:
+        tickets = []
+        for i in range(24):
+            n = int(rng.integers(1, shared.size + 1))
+            ok = torch.empty(n, dtype=torch.int32, device="cuda")
+            ov = torch.empty(n, dtype=torch.int32, device="cuda")
+            tickets.append(srv.submit("sort_by_key", "uint", dk, values=dv, out=ok, out_values=ov, n=n,
+                                      device=True))
+            outs.append((n, ok, ov))
+        os_ = torch.empty(shared.size, dtype=torch.int32, device="cuda")
+        tickets.append(srv.submit("exclusive_scan", "uint", dk, out=os_, device=True))
+        for t in tickets:
+            srv.wait(t)
+    assert np.array_equal(dk.cpu().numpy().view(np.uint32), shared)
+    for n, ok, ov in outs:
+        rk, rv = oracle.radix_sort(shared[:n], "uint", values=np.arange(n, dtype=np.uint32))
+        assert np.array_equal(ok.cpu().numpy().view(np.uint32), rk)
+        assert np.array_equal(ov.cpu().numpy().view(np.uint32), rv)
+    assert np.array_equal(os_.cpu().numpy().view(np.uint32), oracle.scan(shared, "uint", exclusive=True))
