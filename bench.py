@@ -207,8 +207,10 @@ def main():
     ap.add_argument("--impl", default="bcx", choices=["bcx", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "sort", "prims"],
-                    help="'sort' skips the other primitives, 'prims' skips the sort (profiling runs)")
+    ap.add_argument("--only", default="all", choices=["all", "sort", "prims", "precision", "serve", "segmented"],
+                    help="'sort' skips the other sections; 'prims', 'precision', 'serve', 'segmented' run a "
+                         "2^20 sort and that section only (profiling runs)")
+    ap.add_argument("--serve-count", type=int, default=1000, help="requests per arrival rate")
     ap.add_argument("--n-sort", type=int, default=DEFAULT_N_SORT, help="pairs per sort (default 2^28)")
     ap.add_argument("--n-scan", type=int, default=DEFAULT_N_SCAN, help="scan/reduce elements (default 2^30)")
     args = ap.parse_args()
@@ -224,7 +226,7 @@ def main():
     global N_SORT, N_SCAN
     N_SORT = args.n_sort
     N_SCAN = args.n_scan
-    if args.only == "prims":
+    if args.only in ("prims", "precision", "serve", "segmented"):
         N_SORT = 1 << 20
     rank, world, local = dist_init(args.gpus)
     torch.cuda.set_device(local)
@@ -284,10 +286,19 @@ def main():
     # ---- other primitives of the configuration ----------------------------
     prims = {}
     psteps = max(3, min(args.steps, 10))
-    if args.only == "sort":
+    if args.only != "all" and args.only != "prims":
         psteps = 0
     if psteps:
         prims = run_primitives(torch, bc, dev, g, psteps, hbm)
+    precision = None
+    if args.only in ("all", "precision"):
+        precision = run_precision(torch, bc, dev, hbm)
+    segmented = None
+    if args.only in ("all", "segmented"):
+        segmented = run_segmented(torch, bc, dev, hbm)
+    serving = None
+    if args.only in ("all", "serve") and world == 1:
+        serving = run_serving(torch, bc, dev, count=args.serve_count)
 
     # ---- e2e through the C ABI host-buffer entry point ---------------------
     e2e = None
@@ -307,7 +318,8 @@ def main():
                            "l2": "inputs larger than L2: every step sorts its own buffer",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "sorted_check": sorted_ok, "roofline": roofline, "kernel_share": kernel_share,
-                "gpu_launches": launches, "primitives": prims, "e2e": e2e, "cpu_baseline": cpu,
+                "gpu_launches": launches, "primitives": prims, "precision": precision, "segmented": segmented, "serving": serving, "e2e": e2e,
+                "cpu_baseline": cpu,
                 "clocks": clocks.summary()}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -361,6 +373,506 @@ def run_e2e(torch, bc, rank, world):
             "h2d_bytes_per_step": 8 * N_SORT, "d2h_bytes_per_step": 8 * N_SORT,
             "ms_per_step": tot / e2e_steps * 1e3, "steps": e2e_steps,
             "path": "bcx_sort_pairs_host (pinned host buffers)"}
+
+
+# ---- precision and key-distribution stress ---------------------------------
+def run_precision(torch, bc, dev, hbm, seed=20261206, n_acc=1 << 30, n_sort=1 << 27, steps=3):
+    """accumulate / inclusive_scan of 2^30 float32 N(1000, 1): compensated
+    (Neumaier in FP32, FP64 combine) against plain FP32, errors against an
+    FP64 reference computed on the device (torch float64), plus the error of a
+    strictly serial FP32 left fold (what the reference's float accumulate
+    computes).  Then float32 sorts of 2^27 keys with 1% NaN, +-0.0, denormals
+    and +-inf, and uint64 sorts of 2^27 keys: Zipf(1.1), all equal, presorted
+    and 8 significant bits (throughput; order checked by a sortedness scan)."""
+    import numpy as np
+    g = torch.Generator(device=dev).manual_seed(seed)
+    out = {}
+    x = torch.randn(n_acc, dtype=torch.float32, device=dev, generator=g) + 1000.0
+    ref = float(x.double().sum().item())
+    comp = bc.accumulate(x, 0.0, compensated=True)
+    plain = float(bc.reduce(x, compensated=False).item())
+    ms_comp = time_primitive(torch, lambda: bc.reduce(x, compensated=True), steps, 3)
+    ms_plain = time_primitive(torch, lambda: bc.reduce(x, compensated=False), steps, 3)
+    xs = x.cpu().numpy()
+    serial = float(np.cumsum(xs, dtype=np.float32)[-1])  # strict left-to-right FP32 fold
+    del xs
+    out["accumulate_f32_N1000_2p30"] = {
+        "fp64_sum": ref, "compensated": comp, "plain_fp32": plain, "serial_fp32": serial,
+        "rel_err_compensated": abs(comp - ref) / abs(ref), "rel_err_plain_fp32": abs(plain - ref) / abs(ref),
+        "rel_err_serial_fp32": abs(serial - ref) / abs(ref),
+        "ulp_of_fp32_result": float(np.spacing(np.float32(ref))),
+        "abs_err_compensated_in_ulps": abs(comp - ref) / float(np.spacing(np.float32(ref))),
+        "ms_compensated": ms_comp, "ms_plain": ms_plain,
+        "GB_per_s_compensated": 4 * n_acc / ms_comp / 1e6, "frac_compensated": 4 * n_acc / ms_comp / 1e6 / hbm}
+    y = torch.empty_like(x)
+    bc.inclusive_scan(x, out=y, compensated=True)
+    ref_scan = torch.cumsum(x.double(), 0)
+    rel = ((y.double() - ref_scan).abs() / ref_scan.abs())
+    err_c = float(rel.max().item())
+    bc.inclusive_scan(x, out=y, compensated=False)
+    rel = ((y.double() - ref_scan).abs() / ref_scan.abs())
+    err_p = float(rel.max().item())
+    del rel, ref_scan
+    ms_c = time_primitive(torch, lambda: bc.inclusive_scan(x, out=y, compensated=True), steps, 3)
+    ms_p = time_primitive(torch, lambda: bc.inclusive_scan(x, out=y, compensated=False), steps, 3)
+    out["inclusive_scan_f32_N1000_2p30"] = {
+        "max_rel_err_compensated": err_c, "max_rel_err_plain_fp32": err_p, "ms_compensated": ms_c,
+        "ms_plain": ms_p, "GB_per_s_compensated": 8 * n_acc / ms_c / 1e6,
+        "frac_compensated": 8 * n_acc / ms_c / 1e6 / hbm}
+    del x, y
+    torch.cuda.empty_cache()
+
+    def time_sort(make, dtype, label, check_key):
+        base = make()
+        bufs = [base.clone() for _ in range(steps + 1)]
+        bc.sort(bufs[0], dtype=dtype)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for i in range(1, steps + 1):
+            bc.sort(bufs[i], dtype=dtype)
+        b.record()
+        b.synchronize()
+        ms = a.elapsed_time(b) / steps
+        k = check_key(bufs[-1])
+        ok = bool((k[1:] >= k[:-1]).all())
+        del bufs, base, k
+        torch.cuda.empty_cache()
+        out[label] = {"ms": ms, "Gkeys_per_s": n_sort / ms / 1e6, "sorted": ok}
+
+    def f32_stress():
+        v = torch.randn(n_sort, dtype=torch.float32, device=dev, generator=g) * 1e3
+        r = torch.rand(n_sort, device=dev, generator=g)
+        v[r < 0.01] = float("nan")
+        v[(r >= 0.01) & (r < 0.02)] = 0.0
+        v[(r >= 0.02) & (r < 0.03)] = -0.0
+        v[(r >= 0.03) & (r < 0.04)] = 1e-40
+        v[(r >= 0.04) & (r < 0.05)] = -1e-40
+        v[(r >= 0.05) & (r < 0.055)] = float("inf")
+        v[(r >= 0.055) & (r < 0.06)] = -float("inf")
+        return v
+
+    def f32_order_key(t):
+        # the total order of the sort: sign-flipped bits compared as unsigned
+        u = t.view(torch.int32).to(torch.int64) & 0xFFFFFFFF
+        neg = u >= 0x80000000
+        return torch.where(neg, 0xFFFFFFFF - u, u + 0x80000000)
+
+    time_sort(f32_stress, "float", "sort_f32_specials_2p27", f32_order_key)
+
+    def u64(kind):
+        def make():
+            if kind == "zipf":
+                z = np.random.default_rng(seed).zipf(1.1, size=n_sort).astype(np.int64)  # >= 1
+                return torch.from_numpy(z).to(dev)
+            if kind == "equal":
+                return torch.full((n_sort,), 0x123456789, dtype=torch.int64, device=dev)
+            if kind == "sorted":
+                return torch.arange(n_sort, dtype=torch.int64, device=dev) * 3
+            return torch.randint(0, 256, (n_sort,), dtype=torch.int64, device=dev, generator=g)
+        return make
+
+    def u64_key(t):  # values here are non-negative, so signed order is unsigned order
+        return t
+
+    for kind in ("zipf", "equal", "sorted", "8bit"):
+        time_sort(u64(kind), "ulong", f"sort_u64_{kind}_2p27", u64_key)
+    return out
+
+
+# ---- segmented work --------------------------------------------------------
+def segment_offsets(nseg=10_000, lo=16, hi=1 << 20, seed=20261205, total_cap=None):
+    """10,000 segment sizes log-uniform in [16, 2^20] (seeded); with total_cap,
+    the first segments whose sizes reach that total."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), size=nseg)).astype(np.int64)
+    if total_cap is not None:
+        csum = np.cumsum(sizes)
+        k = int(np.searchsorted(csum, total_cap)) + 1
+        sizes = sizes[:k]
+    return np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+
+
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _graph_of(torch, fn):
+    """fn() captured once in a CUDA graph (after one eager warm-up call)."""
+    fn()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    torch.cuda.synchronize()
+    return g
+
+
+def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205):
+    """Segmented sort_by_key (uint32/uint32), segmented exclusive_scan (int32)
+    and reduce_by_key (float32 N(0,1), keys = segment ids) over 10,000
+    log-uniform segments: one launch sequence each, tuned by the autotuner and
+    replayed from a captured CUDA graph, against one plain call per segment on
+    the same stream."""
+    import ctypes as C
+
+    import numpy as np
+
+    from compute_gb300._lib import DTYPES, lib
+    L = lib()
+    results = {}
+    for label, cap in (("10000_segments", None), ("2^28_total", 1 << 28)):
+        offsets = segment_offsets(total_cap=cap, seed=seed)
+        nseg = offsets.size - 1
+        n = int(offsets[-1])
+        sizes = np.diff(offsets).astype(np.int64)
+        offs = torch.from_numpy(offsets.view(np.int64).copy()).to(dev)
+        st = torch.cuda.current_stream().cuda_stream
+        g = torch.Generator(device=dev).manual_seed(seed)
+        entry = {"segments": int(nseg), "elements": n, "min_segment": int(sizes.min()),
+                 "max_segment": int(sizes.max())}
+        rep = C.create_string_buffer(1 << 14)
+
+        # -- segmented sort_by_key uint32 / uint32
+        keys0 = torch.randint(-2**31, 2**31 - 1, (n,), dtype=torch.int32, device=dev, generator=g)
+        vals0 = torch.arange(n, dtype=torch.int32, device=dev)
+        keys, vals = keys0.clone(), vals0.clone()
+        t0 = time.perf_counter()
+        rc = L.bcx_tune_segmented_sort_pairs(st, DTYPES["uint"], 4, keys0.data_ptr(), vals0.data_ptr(), n,
+                                             offs.data_ptr(), nseg, rep, len(rep))
+        assert rc == 0, L.bcx_last_error_string()
+        tune_s = time.perf_counter() - t0
+        tuned = [ln for ln in rep.value.decode().splitlines() if "->" in ln]
+        tb = C.c_size_t(0)
+        L.bcx_segmented_sort_pairs(st, DTYPES["uint"], 4, None, None, n, offs.data_ptr(), nseg, 0, None,
+                                   C.byref(tb))
+        temp = torch.empty(tb.value, dtype=torch.uint8, device=dev)
+
+        def seg_sort():
+            t = C.c_size_t(temp.numel())
+            r = L.bcx_segmented_sort_pairs(torch.cuda.current_stream().cuda_stream, DTYPES["uint"], 4,
+                                           keys.data_ptr(), vals.data_ptr(), n, offs.data_ptr(), nseg, 0,
+                                           temp.data_ptr(), C.byref(t))
+            assert r == 0, L.bcx_last_error_string()
+
+        graph = _graph_of(torch, seg_sort)
+        ms = []
+        for _ in range(steps):
+            keys.copy_(keys0)
+            vals.copy_(vals0)
+            a, b = _events(torch)
+            a.record()
+            graph.replay()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        graph_ms = statistics.median(ms)
+        # correctness: every segment non-decreasing (as uint32)
+        k64 = keys.to(torch.int64) & 0xFFFFFFFF
+        inner = torch.ones(n, dtype=torch.bool, device=dev)
+        inner[offs[:-1].clamp(max=n - 1)] = False
+        ok = bool(((k64[1:] >= k64[:-1]) | ~inner[1:]).all())
+        del k64, inner
+        # one plain sort_by_key per segment
+        keys.copy_(keys0)
+        vals.copy_(vals0)
+        torch.cuda.synchronize()
+        kp, vp = keys.data_ptr(), vals.data_ptr()
+        a, b = _events(torch)
+        a.record()
+        for s_, m in zip(offsets[:-1].tolist(), sizes.tolist()):
+            L.bcx_sort_pairs(st, DTYPES["uint"], 4, kp + 4 * s_, vp + 4 * s_, m, 0, None, None)
+        b.record()
+        b.synchronize()
+        plain_ms = a.elapsed_time(b)
+        small_tile = 4096
+        for ln in tuned:
+            if "small_tile" in ln:
+                small_tile = int(ln.split("->")[1])
+        large = int(sizes[sizes > small_tile].sum())
+        alg_bytes = 68 * large + 16 * (n - large)
+        entry["sort_by_key_u32"] = {
+            "graph_ms": graph_ms, "per_segment_plain_ms": plain_ms, "speedup_vs_plain": plain_ms / graph_ms,
+            "Gkeys_per_s": n / graph_ms / 1e6, "algorithmic_bytes": alg_bytes,
+            "GB_per_s": alg_bytes / graph_ms / 1e6, "frac": alg_bytes / graph_ms / 1e6 / hbm,
+            "segments_sorted": ok, "tuned": tuned, "tune_s": tune_s}
+        del keys0, vals0, keys, vals, temp, graph
+        torch.cuda.empty_cache()
+
+        # -- segmented exclusive_scan int32
+        x = torch.randint(0, 100, (n,), dtype=torch.int32, device=dev, generator=g)
+        out = torch.empty_like(x)
+        rc = L.bcx_tune_segmented_scan(st, DTYPES["int"], x.data_ptr(), n, offs.data_ptr(), nseg, rep, len(rep))
+        assert rc == 0, L.bcx_last_error_string()
+        tuned = [ln for ln in rep.value.decode().splitlines() if "->" in ln]
+        zero = (C.c_ubyte * 8)()
+        L.bcx_segmented_scan(st, DTYPES["int"], 0, 1, zero, x.data_ptr(), out.data_ptr(), n, offs.data_ptr(), nseg,
+                             0, None, C.byref(tb))
+        temp = torch.empty(max(tb.value, 1), dtype=torch.uint8, device=dev)
+
+        def seg_scan():
+            t = C.c_size_t(temp.numel())
+            r = L.bcx_segmented_scan(torch.cuda.current_stream().cuda_stream, DTYPES["int"], 0, 1, zero,
+                                     x.data_ptr(), out.data_ptr(), n, offs.data_ptr(), nseg, 0, temp.data_ptr(),
+                                     C.byref(t))
+            assert r == 0, L.bcx_last_error_string()
+
+        graph = _graph_of(torch, seg_scan)
+        ms = []
+        for _ in range(steps):
+            a, b = _events(torch)
+            a.record()
+            graph.replay()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        graph_ms = statistics.median(ms)
+        xp, op_ = x.data_ptr(), out.data_ptr()
+        a, b = _events(torch)
+        a.record()
+        for s_, m in zip(offsets[:-1].tolist(), sizes.tolist()):
+            L.bcx_scan(st, DTYPES["int"], 0, 1, zero, xp + 4 * s_, op_ + 4 * s_, m, 0, None, None)
+        b.record()
+        b.synchronize()
+        plain_ms = a.elapsed_time(b)
+        entry["exclusive_scan_i32"] = {
+            "graph_ms": graph_ms, "per_segment_plain_ms": plain_ms, "speedup_vs_plain": plain_ms / graph_ms,
+            "GB_per_s": 8 * n / graph_ms / 1e6, "frac": 8 * n / graph_ms / 1e6 / hbm, "tuned": tuned}
+        del x, out, temp, graph
+        torch.cuda.empty_cache()
+
+        # -- reduce_by_key float32 N(0,1), keys = segment ids
+        seg_id = torch.repeat_interleave(torch.arange(nseg, dtype=torch.int32, device=dev),
+                                         torch.from_numpy(sizes).to(dev))
+        v = torch.randn(n, dtype=torch.float32, device=dev, generator=g)
+        ko = torch.empty(nseg, dtype=torch.int32, device=dev)
+        vo = torch.empty(nseg, dtype=torch.float32, device=dev)
+        runs = torch.zeros(1, dtype=torch.int64, device=dev)
+        L.bcx_reduce_by_key(st, DTYPES["int"], DTYPES["float"], 0, seg_id.data_ptr(), v.data_ptr(), n,
+                            ko.data_ptr(), vo.data_ptr(), runs.data_ptr(), 1, None, C.byref(tb))
+        temp = torch.empty(max(tb.value, 1), dtype=torch.uint8, device=dev)
+
+        def rbk():
+            t = C.c_size_t(temp.numel())
+            r = L.bcx_reduce_by_key(torch.cuda.current_stream().cuda_stream, DTYPES["int"], DTYPES["float"], 0,
+                                    seg_id.data_ptr(), v.data_ptr(), n, ko.data_ptr(), vo.data_ptr(),
+                                    runs.data_ptr(), 1, temp.data_ptr(), C.byref(t))
+            assert r == 0, L.bcx_last_error_string()
+
+        graph = _graph_of(torch, rbk)
+        ms = []
+        for _ in range(steps):
+            a, b = _events(torch)
+            a.record()
+            graph.replay()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        graph_ms = statistics.median(ms)
+        runs_ok = int(runs.item()) == nseg
+        # the offset-based segmented reduce (autotuned grid), same sums
+        rc = L.bcx_tune_segmented_reduce(st, DTYPES["float"], v.data_ptr(), offs.data_ptr(), nseg, rep, len(rep))
+        assert rc == 0, L.bcx_last_error_string()
+        tuned = [ln for ln in rep.value.decode().splitlines() if "->" in ln]
+        so = torch.empty(nseg, dtype=torch.float32, device=dev)
+        zf = (C.c_ubyte * 8)()
+        L.bcx_segmented_reduce(st, DTYPES["float"], 0, v.data_ptr(), offs.data_ptr(), nseg, zf, None, 1, None,
+                               C.byref(tb))
+        temp2 = torch.empty(max(tb.value, 1), dtype=torch.uint8, device=dev)
+
+        def segred():
+            t = C.c_size_t(temp2.numel())
+            r = L.bcx_segmented_reduce(torch.cuda.current_stream().cuda_stream, DTYPES["float"], 0, v.data_ptr(),
+                                       offs.data_ptr(), nseg, zf, so.data_ptr(), 1, temp2.data_ptr(), C.byref(t))
+            assert r == 0, L.bcx_last_error_string()
+
+        graph2 = _graph_of(torch, segred)
+        ms = []
+        for _ in range(steps):
+            a, b = _events(torch)
+            a.record()
+            graph2.replay()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        segred_ms = statistics.median(ms)
+        # one plain (compensated) reduce per segment
+        vp_ = v.data_ptr()
+        po = so.data_ptr()
+        a, b = _events(torch)
+        a.record()
+        for i, (s_, m) in enumerate(zip(offsets[:-1].tolist(), sizes.tolist())):
+            L.bcx_reduce(st, DTYPES["float"], 0, vp_ + 4 * s_, m, po + 4 * i, 1, None, None)
+        b.record()
+        b.synchronize()
+        plain_ms = a.elapsed_time(b)
+        entry["reduce_by_key_f32"] = {
+            "graph_ms": graph_ms, "per_segment_plain_ms": plain_ms, "speedup_vs_plain": plain_ms / graph_ms,
+            "GB_per_s": 8 * n / graph_ms / 1e6, "frac": 8 * n / graph_ms / 1e6 / hbm, "runs_ok": runs_ok,
+            "segmented_reduce_by_offsets_ms": segred_ms,
+            "segmented_reduce_GB_per_s": 4 * n / segred_ms / 1e6, "tuned": tuned}
+        del seg_id, v, ko, vo, runs, temp, temp2, so, graph, graph2
+        torch.cuda.empty_cache()
+        results[label] = entry
+    return results
+
+
+# ---- serving loop ----------------------------------------------------------
+SERVE_KINDS = ("sort_by_key", "exclusive_scan", "reduce")
+SERVE_DTYPES = ("int", "uint", "float", "ulong")
+SERVE_RATES = (1000, 3000, 10000, 30000, 100000)
+
+
+def make_serving_requests(count, seed, lo=10, hi=26):
+    """Seeded request stream: 50% sort_by_key, 30% exclusive_scan, 20% reduce;
+    n log-uniform in [2^lo, 2^hi]; dtype uniform over int/uint/float/ulong."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    kinds = rng.choice(3, size=count, p=[0.5, 0.3, 0.2])
+    dtypes = rng.integers(0, 4, size=count)
+    ns = np.exp(rng.uniform(np.log(2.0 ** lo), np.log(2.0 ** hi), size=count)).astype(np.int64)
+    offs = rng.integers(0, 1 << 20, size=count) * 64  # element offset into the input pool (64-aligned)
+    return kinds, dtypes, ns, offs
+
+
+def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo=10, hi=26, slots=8):
+    """Open-loop Poisson arrivals of device-resident requests through the
+    continuous-batching server, against the same requests issued as serial
+    plain C-ABI calls (each waited for before the next, as a caller that needs
+    its result does) and as plain calls queued back to back on one stream."""
+    import ctypes as C
+
+    import numpy as np
+
+    from compute_gb300._lib import DTYPES, DTYPE_SIZE, Request, lib
+    from compute_gb300.serve import Server
+    L = lib()
+    kinds, dtypes, ns, offs = make_serving_requests(count, seed, lo, hi)
+    pool_n = (1 << hi) + (1 << 20) * 64
+    gen = torch.Generator(device=dev).manual_seed(seed)
+    pools = {}
+    for name in SERVE_DTYPES:
+        if name == "float":
+            pools[name] = torch.rand(pool_n, dtype=torch.float32, device=dev, generator=gen)
+        elif name == "ulong":
+            pools[name] = torch.randint(-2**63, 2**63 - 1, (pool_n,), dtype=torch.int64, device=dev, generator=gen)
+        else:
+            pools[name] = torch.randint(-2**31, 2**31 - 1, (pool_n,), dtype=torch.int32, device=dev, generator=gen)
+    vals = torch.arange(pool_n, dtype=torch.int32, device=dev)
+    # Output arena: every request gets its own output slices.
+    sizes = []
+    for k, d, n in zip(kinds, dtypes, ns):
+        es = DTYPE_SIZE[SERVE_DTYPES[d]]
+        if k == 0:
+            sizes.append((n * es + 255) // 256 * 256 + (n * 4 + 255) // 256 * 256)
+        elif k == 1:
+            sizes.append((n * es + 255) // 256 * 256)
+        else:
+            sizes.append(256)
+    arena = torch.empty(int(sum(sizes)), dtype=torch.uint8, device=dev)
+    base = arena.data_ptr()
+    reqs, elems, bytes_moved = [], 0, 0
+    cur = base
+    for k, d, n, o, sz in zip(kinds, dtypes, ns, offs, sizes):
+        name = SERVE_DTYPES[d]
+        es = DTYPE_SIZE[name]
+        n = int(n)
+        src = pools[name].data_ptr() + int(o) * es
+        if k == 0:
+            ov = cur + (n * es + 255) // 256 * 256
+            r = Request(0, DTYPES[name], 4, n, 1, src, vals.data_ptr() + int(o) * 4, cur, ov)
+            bytes_moved += n * (es + 4) * 2
+        elif k == 1:
+            r = Request(1, DTYPES[name], 0, n, 1, src, None, cur, None)
+            bytes_moved += n * es * 2
+        else:
+            r = Request(2, DTYPES[name], 0, n, 1, src, None, cur, None)
+            bytes_moved += n * es
+        reqs.append(r)
+        elems += n
+        cur += int(sz)
+    torch.cuda.synchronize()
+
+    # -- serial plain calls through the C ABI on one stream
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    zero = (C.c_ubyte * 8)()
+    DTYPE_SIZE_BY_CODE = {DTYPES[k]: DTYPE_SIZE[k] for k in SERVE_DTYPES}
+
+    def plain(r):
+        if r.kind == 0:
+            es = DTYPE_SIZE_BY_CODE[r.dtype]
+            L.bcx_memcpy_async(r.out, r.keys, r.n * es, stream)
+            L.bcx_memcpy_async(r.out_values, r.values, r.n * 4, stream)
+            return L.bcx_sort_pairs(stream, r.dtype, 4, r.out, r.out_values, r.n, 0, None, None)
+        comp = 1 if r.dtype == DTYPES["float"] else 0
+        if r.kind == 1:
+            return L.bcx_scan(stream, r.dtype, 0, 1, zero, r.keys, r.out, r.n, comp, None, None)
+        return L.bcx_reduce(stream, r.dtype, 0, r.keys, r.n, r.out, comp, None, None)
+
+    for r in reqs[:20]:
+        assert plain(r) == 0
+    L.bcx_stream_synchronize(stream)
+    per_call = []
+    t0 = time.perf_counter()
+    for r in reqs:
+        a = time.perf_counter()
+        rc = plain(r)
+        L.bcx_stream_synchronize(stream)
+        per_call.append(time.perf_counter() - a)
+        assert rc == 0
+    serial_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for r in reqs:
+        plain(r)
+    L.bcx_stream_synchronize(stream)
+    queued_s = time.perf_counter() - t0
+    per_call_ms = np.array(per_call) * 1e3
+    out = {"requests_per_rate": count, "elements": int(elems), "bytes_per_pass": int(bytes_moved),
+           "mix": "50% sort_by_key (values uint32) / 30% exclusive_scan / 20% reduce; "
+                  f"n log-uniform [2^{lo}, 2^{hi}]; dtype uniform int32/uint32/float32/uint64; "
+                  "device-resident inputs, per-request outputs",
+           "serial_plain": {"req_per_s": count / serial_s, "GB_per_s": bytes_moved / serial_s / 1e9,
+                            "p50_ms": float(np.percentile(per_call_ms, 50)),
+                            "p99_ms": float(np.percentile(per_call_ms, 99)),
+                            "note": "one plain C-ABI call per request, each waited for"},
+           "queued_plain": {"req_per_s": count / queued_s, "GB_per_s": bytes_moved / queued_s / 1e9,
+                            "note": "the same plain calls back to back on one stream, one wait at the end"},
+           "rates": []}
+
+    # -- the server, open-loop Poisson arrivals
+    rng = np.random.default_rng(seed + 1)
+    with Server(slots=slots) as srv:
+        for r in reqs[:20]:
+            srv.wait(srv.submit_request(r))
+        for rate in rates:
+            srv.reset_stats()
+            gaps = rng.exponential(1.0 / rate, size=count)
+            arrivals = np.cumsum(gaps)
+            tickets = [0] * count
+            t0 = time.perf_counter()
+            for i, r in enumerate(reqs):
+                target = t0 + arrivals[i]
+                while time.perf_counter() < target:
+                    pass
+                tickets[i] = srv.submit_request(r)
+            lat = np.array([srv.wait(t) for t in tickets])
+            t_end = max(t0 + arrivals[i] + lat[i] / 1e3 for i in range(count))
+            span = t_end - t0
+            st = srv.stats()
+            out["rates"].append({
+                "offered_req_per_s": rate, "achieved_req_per_s": count / span,
+                "GB_per_s": bytes_moved / span / 1e9,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "max_ms": float(lat.max()), "batches": int(st["batches"]),
+                "batched_requests": int(st["batched_requests"])})
+    best = max(x["achieved_req_per_s"] for x in out["rates"])
+    out["server_best_req_per_s"] = best
+    out["speedup_vs_serial_plain"] = best / out["serial_plain"]["req_per_s"]
+    out["speedup_vs_queued_plain"] = best / out["queued_plain"]["req_per_s"]
+    del arena, pools, vals
+    torch.cuda.empty_cache()
+    return out
 
 
 if __name__ == "__main__":

@@ -83,6 +83,13 @@ SIGNATURES = {
     "bcx_jit_cache_stats": (_i, [C.POINTER(C.c_uint64)] * 5),
     "bcx_jit_cache_configure": (_i, [_sz, _i]),
     "bcx_device_sm_count": (_i, [C.POINTER(_i)]),
+    "bcx_param_get": (_i, [C.c_char_p, C.c_char_p, C.c_uint, C.POINTER(C.c_uint)]),
+    "bcx_param_set": (_i, [C.c_char_p, C.c_char_p, C.c_uint]),
+    "bcx_param_save": (_i, []),
+    "bcx_param_clear": (_i, []),
+    "bcx_tune_segmented_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _vp, _sz, C.c_char_p, _sz]),
+    "bcx_tune_segmented_scan": (_i, [_vp, _i, _vp, _sz, _vp, _sz, C.c_char_p, _sz]),
+    "bcx_tune_segmented_reduce": (_i, [_vp, _i, _vp, _vp, _sz, C.c_char_p, _sz]),
     "bcx_profile_enable": (_i, [_i]),
     "bcx_profile_reset": (_i, []),
     "bcx_profile_read": (_i, [C.c_char_p, _sz, C.POINTER(C.c_uint64), C.POINTER(C.c_double), _sz, _szp]),

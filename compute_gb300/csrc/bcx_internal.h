@@ -45,6 +45,7 @@ bcx_status current_device_state(DeviceState **out);
 
 size_t dtype_size(bcx_dtype t);
 bool dtype_valid(int t);
+const char *dtype_name(bcx_dtype t);  // OpenCL C spelling: "int", "ulong", ...
 
 // Bytes rounded up to a 256-byte boundary (alignment of every sub-buffer
 // carved out of a temporary allocation).
@@ -87,5 +88,28 @@ bool profiling_enabled();
 
 // Checks the launch that just happened.
 bcx_status launch_status(const char *kernel);
+
+// Tuning parameters of the current device (bcx_tune.cpp): the stored value of
+// (object, parameter), or default_value when none is stored.
+uint32_t param_get(const std::string &object, const char *parameter, uint32_t default_value);
+void param_set(const std::string &object, const char *parameter, uint32_t value);
+bcx_status param_save();
+// Largest small-segment tile the segmented sort is compiled for with these
+// key and value sizes (bcx_segmented_sort.cu).
+uint32_t segsort_small_tile_limit(size_t key_bytes, size_t value_bytes);
+
+// One piece of a batched gather/scatter: `bytes` bytes from src to dst, both
+// device-accessible.  The request server splits every buffer it moves into
+// pieces of at most kCopyChunkBytes so that one launch of copy_chunks (one
+// block per piece) moves the buffers of a whole batch.
+struct CopyChunk {
+  const void *src;
+  void *dst;
+  uint64_t bytes;
+  uint64_t reserved;
+};
+constexpr size_t kCopyChunkBytes = size_t(64) << 10;
+// chunks: device array of `count` pieces.
+bcx_status copy_chunks(const CopyChunk *chunks, size_t count, cudaStream_t s);
 
 }  // namespace bcx

@@ -76,6 +76,11 @@ size_t dtype_size(bcx_dtype t) {
 
 bool dtype_valid(int t) { return t >= BCX_CHAR && t <= BCX_DOUBLE; }
 
+const char *dtype_name(bcx_dtype t) {
+  static const char *names[] = {"char", "uchar", "short", "ushort", "int", "uint", "long", "ulong", "float", "double"};
+  return dtype_valid(int(t)) ? names[int(t)] : "invalid";
+}
+
 TempStorage::~TempStorage() {
   if (owned_ && ptr_) cudaFreeAsync(ptr_, stream_);
 }

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <string>
 #include <type_traits>
 
 #include "bcx.h"
@@ -31,8 +32,8 @@ namespace {
 
 constexpr int kSegThreads = 256;
 constexpr int kSegWarps = kSegThreads / kWarp;
-constexpr int kSegItems = 8;
-constexpr int kSegTile = kSegThreads * kSegItems;
+constexpr int kSegItems = 8;  // default items per thread of the segmented scan
+constexpr int kSegTile = kSegThreads * kSegItems;  // segmented reduce stride
 enum : uint32_t { kSgInvalid = 0, kSgAggregate = 1, kSgPrefix = 2 };
 
 template <class T, template <class> class OpT>
@@ -127,24 +128,25 @@ __device__ __forceinline__ size_t lower_bound_u64(const unsigned long long *offs
   return lo;
 }
 
-template <class T, class P>
+template <class T, class P, int ITEMS>
 __global__ void __launch_bounds__(kSegThreads)
 segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
                       const unsigned long long *__restrict__ offsets, size_t nseg, int exclusive,
                       typename P::Acc init, SgStatus<P> st, uint32_t *__restrict__ tile_counter,
                       uint32_t *err) {
   typedef Sg<P> S;
-  __shared__ uint32_t s_heads[kSegTile / 32];
+  constexpr int TILE = kSegThreads * ITEMS;
+  __shared__ uint32_t s_heads[TILE / 32];
   __shared__ S s_warp[kSegWarps];
   __shared__ S s_prefix;
   __shared__ uint32_t s_tile;
   const unsigned lane = lane_id(), warp = threadIdx.x / kWarp;
-  for (int i = threadIdx.x; i < kSegTile / 32; i += kSegThreads) s_heads[i] = 0;
+  for (int i = threadIdx.x; i < TILE / 32; i += kSegThreads) s_heads[i] = 0;
   if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
   __syncthreads();
   const size_t tile = s_tile;
-  const size_t tile_base = tile * kSegTile;
-  const size_t tile_end = (tile_base + kSegTile < n) ? tile_base + kSegTile : n;
+  const size_t tile_base = tile * TILE;
+  const size_t tile_end = (tile_base + TILE < n) ? tile_base + TILE : n;
   // Mark the segment starts inside this tile (offsets[0..nseg] are starts;
   // offsets[nseg] == n is not).
   if (warp == 0) {
@@ -157,17 +159,17 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
     }
   }
   __syncthreads();
-  const uint32_t warp_first = warp * (kWarp * kSegItems);
-  T x[kSegItems];
+  const uint32_t warp_first = warp * (kWarp * ITEMS);
+  T x[ITEMS];
 #pragma unroll
-  for (int i = 0; i < kSegItems; ++i) {
+  for (int i = 0; i < ITEMS; ++i) {
     const size_t idx = tile_base + warp_first + i * kWarp + lane;
     x[i] = idx < n ? in[idx] : T(0);
   }
-  S lane_incl[kSegItems];
+  S lane_incl[ITEMS];
   S run = sg_ident<P>();
 #pragma unroll
-  for (int i = 0; i < kSegItems; ++i) {
+  for (int i = 0; i < ITEMS; ++i) {
     const uint32_t local = warp_first + i * kWarp + lane;
     const size_t idx = tile_base + local;
     S e;
@@ -244,7 +246,7 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
     prev_last_valid = 1;
   }
 #pragma unroll
-  for (int i = 0; i < kSegItems; ++i) {
+  for (int i = 0; i < ITEMS; ++i) {
     const uint32_t local = warp_first + i * kWarp + lane;
     const size_t idx = tile_base + local;
     const S incl = sg_comb<P>(pre, lane_incl[i]);
@@ -299,15 +301,39 @@ segmented_reduce_kernel(const T *__restrict__ in, const unsigned long long *__re
   }
 }
 
+// Tile shapes the segmented scan is compiled for: 8 or 16 items per thread
+// for 4-byte elements, 4 or 8 for wider ones (tunable "items_per_thread").
+template <class T> struct SegScanShapes {
+  static constexpr int small = sizeof(T) == 4 ? 8 : 4;
+  static constexpr int large = sizeof(T) == 4 ? 16 : 8;
+};
+
+std::string seg_object(const char *what, bcx_dtype t) { return std::string(what) + "_" + dtype_name(t); }
+
+template <class T, class P, int ITEMS>
+bcx_status launch_segmented_scan(cudaStream_t s, int exclusive, const T &init_v, const void *in, void *out,
+                                 size_t n, const unsigned long long *offsets, size_t nseg, char *base,
+                                 const SgStatus<P> &st, DeviceState *ds) {
+  const size_t tiles = div_up(n, size_t(kSegThreads) * ITEMS);
+  KernelScope ks("segmented_scan", s);
+  segmented_scan_kernel<T, P, ITEMS><<<unsigned(tiles), kSegThreads, 0, s>>>(
+      static_cast<const T *>(in), static_cast<T *>(out), n, offsets, nseg, exclusive, P::from_host(init_v), st,
+      reinterpret_cast<uint32_t *>(base), ds->err_word);
+  return launch_status("segmented_scan");
+}
+
 template <class T, class P>
-bcx_status run_segmented_scan(cudaStream_t s, int exclusive, const void *init, const void *in, void *out,
-                              size_t n, const unsigned long long *offsets, size_t nseg, void *temp,
+bcx_status run_segmented_scan(cudaStream_t s, bcx_dtype type, int exclusive, const void *init, const void *in,
+                              void *out, size_t n, const unsigned long long *offsets, size_t nseg, void *temp,
                               size_t *temp_bytes) {
   typedef Sg<P> S;
+  typedef SegScanShapes<T> Shapes;
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;
-  const size_t tiles = div_up(n, kSegTile);
+  // Storage for the most tiles any compiled shape makes, so the size does not
+  // depend on the tuned shape.
+  const size_t tiles = div_up(n, size_t(kSegThreads) * Shapes::small);
   const size_t need = 256 + align256(tiles * 4) + 2 * align256(tiles * sizeof(S));
   TempStorage ts;
   bool query = false;
@@ -321,16 +347,15 @@ bcx_status run_segmented_scan(cudaStream_t s, int exclusive, const void *init, c
   BCX_CUDA(cudaMemsetAsync(base, 0, 256 + align256(tiles * 4), s));
   T init_v;
   memcpy(&init_v, init, sizeof(T));
-  KernelScope ks("segmented_scan", s);
-  segmented_scan_kernel<T, P><<<unsigned(tiles), kSegThreads, 0, s>>>(
-      static_cast<const T *>(in), static_cast<T *>(out), n, offsets, nseg, exclusive, P::from_host(init_v), st,
-      reinterpret_cast<uint32_t *>(base), ds->err_word);
-  return launch_status("segmented_scan");
+  const uint32_t items = param_get(seg_object("segmented_scan", type), "items_per_thread", uint32_t(Shapes::small));
+  if (items == uint32_t(Shapes::large))
+    return launch_segmented_scan<T, P, Shapes::large>(s, exclusive, init_v, in, out, n, offsets, nseg, base, st, ds);
+  return launch_segmented_scan<T, P, Shapes::small>(s, exclusive, init_v, in, out, n, offsets, nseg, base, st, ds);
 }
 
 template <class T, class P>
-bcx_status run_segmented_reduce(cudaStream_t s, const void *in, const unsigned long long *offsets, size_t nseg,
-                                const void *init, void *out, void *temp, size_t *temp_bytes) {
+bcx_status run_segmented_reduce(cudaStream_t s, bcx_dtype type, const void *in, const unsigned long long *offsets,
+                                size_t nseg, const void *init, void *out, void *temp, size_t *temp_bytes) {
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;
@@ -341,7 +366,8 @@ bcx_status run_segmented_reduce(cudaStream_t s, const void *in, const unsigned l
   BCX_CUDA(cudaMemsetAsync(ts.ptr(), 0, 256, s));
   T init_v;
   memcpy(&init_v, init, sizeof(T));
-  size_t blocks = size_t(ds->sm_count) * 8;
+  const uint32_t per_sm = param_get(seg_object("segmented_reduce", type), "blocks_per_sm", 8u);
+  size_t blocks = size_t(ds->sm_count) * (per_sm ? per_sm : 8u);
   if (blocks > nseg) blocks = nseg;
   KernelScope ks("segmented_reduce", s);
   segmented_reduce_kernel<T, P><<<unsigned(blocks), kSegThreads, 0, s>>>(
@@ -413,7 +439,7 @@ bcx_status bcx_segmented_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int 
   bcx_status rc = seg_dispatch(type, op, compensated, [&](auto *tp, auto *pp) -> bcx_status {
     typedef std::remove_pointer_t<decltype(tp)> T;
     typedef std::remove_pointer_t<decltype(pp)> P;
-    return run_segmented_scan<T, P>((cudaStream_t)stream, exclusive, init_p, in, out, n, offs, nseg, temp,
+    return run_segmented_scan<T, P>((cudaStream_t)stream, type, exclusive, init_p, in, out, n, offs, nseg, temp,
                                     temp_bytes);
   });
   if (rc == BCX_UNSUPPORTED) set_error("segmented scan: dtype %d / functor %d not provided", int(type), int(op));
@@ -434,7 +460,7 @@ bcx_status bcx_segmented_reduce(bcx_stream stream, bcx_dtype type, bcx_op op, co
   bcx_status rc = seg_dispatch(type, op, compensated, [&](auto *tp, auto *pp) -> bcx_status {
     typedef std::remove_pointer_t<decltype(tp)> T;
     typedef std::remove_pointer_t<decltype(pp)> P;
-    return run_segmented_reduce<T, P>((cudaStream_t)stream, in, offs, nseg, init, out, temp, temp_bytes);
+    return run_segmented_reduce<T, P>((cudaStream_t)stream, type, in, offs, nseg, init, out, temp, temp_bytes);
   });
   if (rc == BCX_UNSUPPORTED)
     set_error("segmented reduce: dtype %d / functor %d not provided", int(type), int(op));

@@ -21,6 +21,9 @@
 // tiles of its own segment.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <string>
+
 #include "bcx.h"
 #include "bcx_common.cuh"
 #include "bcx_internal.h"
@@ -34,15 +37,23 @@ using namespace radix;
 constexpr int kPlanThreads = 1024;
 
 // Largest segment the shared-memory path sorts: about 96 KB of double
-// buffered keys and values, at most 4096 pairs.
+// buffered keys and values, at most 4096 pairs.  The path is compiled for
+// tiles of 1024, 2048 and 4096 pairs up to that limit; the tile in use (and
+// with it the size below which a segment is sorted in shared memory) is the
+// tunable "small_tile", the grid the tunable "small_blocks_per_sm".
 template <class U, int VB>
 struct SmallCap {
   typedef typename value_type_of<VB>::type VT;
   static constexpr size_t kPair = sizeof(U) + (VB ? sizeof(VT) : 0);
   static constexpr int raw = int((96 * 1024) / (2 * kPair));
   static constexpr int value = raw >= 4096 ? 4096 : (raw >= 2048 ? 2048 : 1024);
-  static constexpr int IPT = value / kSortThreads;
-  static constexpr size_t kBytes = size_t(kSortWarps) * kRadix * 4 + 2 * size_t(value) * kPair;
+};
+constexpr uint32_t kMinSmallTile = 1024;
+
+template <class U, int VB, int CAP>
+struct SmallTile {
+  static constexpr int IPT = CAP / kSortThreads;
+  static constexpr size_t kBytes = size_t(kSortWarps) * kRadix * 4 + 2 * size_t(CAP) * SmallCap<U, VB>::kPair;
 };
 
 // ---- plan ------------------------------------------------------------------
@@ -241,15 +252,13 @@ __global__ void segsort_copyback_kernel(U *__restrict__ keys_main, const U *__re
 }
 
 // ---- small segments: whole-segment sort in shared memory -------------------
-template <class U, int VB>
+template <class U, int VB, int CAP>
 __global__ void __launch_bounds__(kSortThreads)
 segsort_small_kernel(U *__restrict__ keys, typename value_type_of<VB>::type *__restrict__ vals,
                      const unsigned long long *__restrict__ offsets, uint32_t nseg, int passes,
                      const KeyXform<U> xf, uint32_t *__restrict__ seg_counter) {
   typedef typename value_type_of<VB>::type VT;
-  typedef SmallCap<U, VB> C;
-  constexpr int CAP = C::value;
-  constexpr int IPT = C::IPT;
+  constexpr int IPT = SmallTile<U, VB, CAP>::IPT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t *wcnt = reinterpret_cast<uint32_t *>(smem_raw);
   U *kbuf = reinterpret_cast<U *>(smem_raw + size_t(kSortWarps) * kRadix * 4);  // [2][CAP]
@@ -368,8 +377,9 @@ SegLayout seg_layout(size_t n, size_t nseg) {
   constexpr int PASSES = int(sizeof(U));
   constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
   SegLayout L;
-  const size_t cap = SmallCap<U, VB>::value;
-  L.max_large = uint32_t(std::min<size_t>(nseg, n / (cap + 1) + 1));
+  // sized for the smallest small tile (the most large segments), so the
+  // size does not depend on the tuned tile
+  L.max_large = uint32_t(std::min<size_t>(nseg, n / (kMinSmallTile + 1) + 1));
   L.max_tiles = uint32_t(n / TILE + L.max_large + 1);
   size_t off = 0;
   L.alt_keys = off;
@@ -394,6 +404,32 @@ SegLayout seg_layout(size_t n, size_t nseg) {
   L.zero_begin = L.counters;
   L.zero_bytes = off - L.counters;
   return L;
+}
+
+template <class U, int VB, int CAP>
+bcx_status launch_small(cudaStream_t s, U *k_main, typename value_type_of<VB>::type *v_main,
+                        const unsigned long long *offsets, size_t nseg, const KeyXform<U> &xf, uint32_t *counter,
+                        uint32_t per_sm, const DeviceState *ds) {
+  if constexpr (CAP > SmallCap<U, VB>::value) {
+    return BCX_UNSUPPORTED;
+  } else {
+    constexpr size_t smem = SmallTile<U, VB, CAP>::kBytes;
+    static int resident = 0;  // blocks per SM at this shared-memory size
+    if (!resident) {
+      BCX_CUDA(cudaFuncSetAttribute(segsort_small_kernel<U, VB, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(smem)));
+      int r = 0;
+      BCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, segsort_small_kernel<U, VB, CAP>, kSortThreads,
+                                                             smem));
+      resident = r > 0 ? r : 1;
+    }
+    size_t blocks = size_t(ds->sm_count) * (per_sm ? per_sm : uint32_t(resident));
+    if (blocks > nseg) blocks = nseg;
+    KernelScope ks("segsort_small", s);
+    segsort_small_kernel<U, VB, CAP><<<unsigned(blocks), kSortThreads, smem, s>>>(
+        k_main, v_main, offsets, uint32_t(nseg), int(sizeof(U)), xf, counter);
+    return launch_status("segsort_small");
+  }
 }
 
 template <class U, int VB>
@@ -425,30 +461,23 @@ bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const u
   uint32_t *seg_hist = reinterpret_cast<uint32_t *>(base + L.seg_hist);
   uint32_t *status = reinterpret_cast<uint32_t *>(base + L.status);
   const KeyXform<U> xf = make_xform<U>(kind, desc);
+  const std::string obj = "segmented_sort_k" + std::to_string(8 * sizeof(U)) + "_v" + std::to_string(VB);
+  uint32_t cap = param_get(obj, "small_tile", uint32_t(SmallCap<U, VB>::value));
+  cap = cap >= 4096 ? 4096u : (cap >= 2048 ? 2048u : kMinSmallTile);
+  if (cap > uint32_t(SmallCap<U, VB>::value)) cap = uint32_t(SmallCap<U, VB>::value);
+  const uint32_t per_sm = param_get(obj, "small_blocks_per_sm", 0u);
   BCX_CUDA(cudaMemsetAsync(base + L.zero_begin, 0, L.zero_bytes, s));
   {
     KernelScope ks("segsort_plan", s);
-    segsort_plan_kernel<<<1, kPlanThreads, 0, s>>>(offsets, uint32_t(nseg), uint32_t(SmallCap<U, VB>::value),
-                                                   TILE, tile_first, large_ord, seg_of_large, totals);
+    segsort_plan_kernel<<<1, kPlanThreads, 0, s>>>(offsets, uint32_t(nseg), cap, TILE, tile_first, large_ord,
+                                                   seg_of_large, totals);
     rc = launch_status("segsort_plan");
     if (rc) return rc;
   }
-  {
-    constexpr size_t smem = SmallCap<U, VB>::kBytes;
-    static bool attr = false;
-    if (!attr) {
-      BCX_CUDA(cudaFuncSetAttribute(segsort_small_kernel<U, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    int(smem)));
-      attr = true;
-    }
-    size_t blocks = size_t(ds->sm_count) * 4;
-    if (blocks > nseg) blocks = nseg;
-    KernelScope ks("segsort_small", s);
-    segsort_small_kernel<U, VB><<<unsigned(blocks), kSortThreads, smem, s>>>(k_main, v_main, offsets,
-                                                                              uint32_t(nseg), PASSES, xf, counters);
-    rc = launch_status("segsort_small");
-    if (rc) return rc;
-  }
+  if (cap == 4096) rc = launch_small<U, VB, 4096>(s, k_main, v_main, offsets, nseg, xf, counters, per_sm, ds);
+  else if (cap == 2048) rc = launch_small<U, VB, 2048>(s, k_main, v_main, offsets, nseg, xf, counters, per_sm, ds);
+  else rc = launch_small<U, VB, 1024>(s, k_main, v_main, offsets, nseg, xf, counters, per_sm, ds);
+  if (rc) return rc;
   {
     KernelScope ks("segsort_hist", s);
     segsort_hist_kernel<U, PASSES><<<L.max_tiles, kHistThreads, 0, s>>>(
@@ -502,6 +531,13 @@ bcx_status segsort_vb(cudaStream_t s, size_t vb, void *k, void *v, size_t n, con
 }
 
 }  // namespace
+
+uint32_t segsort_small_tile_limit(size_t key_bytes, size_t value_bytes) {
+  const size_t pair = key_bytes + value_bytes;
+  const size_t raw = (96 * 1024) / (2 * pair);
+  return raw >= 4096 ? 4096u : (raw >= 2048 ? 2048u : 1024u);
+}
+
 }  // namespace bcx
 
 using namespace bcx;

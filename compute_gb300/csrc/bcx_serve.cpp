@@ -58,6 +58,10 @@ struct Batch;
 struct Slot {
   cudaStream_t stream = nullptr;
   bool busy = false;
+  // Page-locked staging for a batch's segment offsets and copy pieces; reused
+  // only after the slot's previous batch has completed.
+  char *stage = nullptr;
+  size_t stage_bytes = 0;
 };
 
 struct Batch {
@@ -126,95 +130,181 @@ void CUDART_CB on_batch_done(void *p) {
   delete b;
 }
 
-// Enqueue one batch on its slot stream.  Called with the server lock held
-// (only enqueues asynchronous work).
-bcx_status launch_batch(bcx_server *srv, Batch *b, size_t temp_bytes) {
+// Runs a batch's operation on device buffers that are already in place:
+// sort sorts (keys, values) in place, scan writes `second`, reduce writes one
+// result per segment to `second`.  k == 1 uses the plain kernels.
+bcx_status run_op(const bcx_request &r0, cudaStream_t s, size_t k, size_t n, void *keys, void *second,
+                  const uint64_t *d_offs, void *tmp, size_t temp_bytes) {
+  // A NULL temp with a size pointer would be a size query: pass no pointer
+  // when the call needs no temporary storage.
+  size_t tb_val = temp_bytes;
+  size_t *tbp = temp_bytes ? &tb_val : nullptr;
+  if (!temp_bytes) tmp = nullptr;
+  const int comp = (r0.dtype == BCX_FLOAT || r0.dtype == BCX_DOUBLE) ? 1 : 0;
+  unsigned char zero[8] = {0};
+  if (r0.kind == BCX_REQ_SORT_PAIRS) {
+    if (k == 1)
+      return r0.value_bytes ? bcx_sort_pairs(s, r0.dtype, r0.value_bytes, keys, second, n, 0, tmp, tbp)
+                            : bcx_sort_keys(s, r0.dtype, keys, n, 0, tmp, tbp);
+    return bcx_segmented_sort_pairs(s, r0.dtype, r0.value_bytes, keys, second, n, d_offs, k, 0, tmp, tbp);
+  }
+  if (r0.kind == BCX_REQ_EXCLUSIVE_SCAN) {
+    if (k == 1) return bcx_scan(s, r0.dtype, BCX_PLUS, 1, zero, keys, second, n, comp, tmp, tbp);
+    return bcx_segmented_scan(s, r0.dtype, BCX_PLUS, 1, zero, keys, second, n, d_offs, k, comp, tmp, tbp);
+  }
+  if (k == 1) return bcx_reduce(s, r0.dtype, BCX_PLUS, keys, n, second, comp, tmp, tbp);
+  return bcx_segmented_reduce(s, r0.dtype, BCX_PLUS, keys, d_offs, k, zero, second, comp, tmp, tbp);
+}
+
+bool device_resident(const bcx_request &r) { return (r.flags & BCX_REQ_DEVICE_RESIDENT) != 0; }
+
+// A lone device-resident request computes straight on the caller's buffers
+// (a sort first copies its inputs to the outputs unless they alias), so its
+// only allocation is the temporary storage.
+bcx_status launch_direct(bcx_server *srv, Batch *b, size_t temp_bytes) {
   cudaStream_t s = srv->slots[b->slot].stream;
+  const bcx_request &r = b->reqs[0]->r;
+  const size_t es = elem_size(r.dtype);
+  if (temp_bytes) BCX_CUDA(cudaMallocAsync(&b->dev, temp_bytes, s));
+  bcx_status rc = BCX_SUCCESS;
+  if (r.n) {
+    if (r.kind == BCX_REQ_SORT_PAIRS) {
+      if (r.out != r.keys) BCX_CUDA(cudaMemcpyAsync(r.out, r.keys, r.n * es, cudaMemcpyDeviceToDevice, s));
+      if (r.value_bytes && r.out_values != r.values)
+        BCX_CUDA(cudaMemcpyAsync(r.out_values, r.values, r.n * r.value_bytes, cudaMemcpyDeviceToDevice, s));
+      rc = run_op(r, s, 1, r.n, r.out, r.out_values, nullptr, b->dev, temp_bytes);
+    } else {
+      rc = run_op(r, s, 1, r.n, const_cast<void *>(r.keys), r.out, nullptr, b->dev, temp_bytes);
+    }
+  } else if (r.kind == BCX_REQ_REDUCE) {
+    BCX_CUDA(cudaMemsetAsync(r.out, 0, es, s));
+  }
+  if (rc)
+    for (auto &q : b->reqs) q->status = rc;
+  if (b->dev) BCX_CUDA(cudaFreeAsync(b->dev, s));
+  BCX_CUDA(cudaLaunchHostFunc(s, on_batch_done, b));
+  return BCX_SUCCESS;
+}
+
+// Appends the pieces that move `bytes` bytes from src to dst.
+void add_pieces(std::vector<CopyChunk> &v, const void *src, void *dst, size_t bytes) {
+  for (size_t o = 0; o < bytes; o += kCopyChunkBytes)
+    v.push_back(CopyChunk{static_cast<const char *>(src) + o, static_cast<char *>(dst) + o,
+                          uint64_t(std::min(kCopyChunkBytes, bytes - o)), 0});
+}
+
+// Enqueue one batch on its slot stream.  Called with the server lock held
+// (only enqueues asynchronous work).  Layout of the batch allocation:
+// keys/input | values or output | offsets + copy pieces | temp.  Host
+// buffers move with one copy per buffer; device-resident buffers move with
+// one gather launch in and one scatter launch out for the whole batch.
+bcx_status launch_batch(bcx_server *srv, Batch *b, size_t temp_bytes) {
+  Slot &slot = srv->slots[b->slot];
+  cudaStream_t s = slot.stream;
   const bcx_request &r0 = b->reqs[0]->r;
-  const size_t es = elem_size(r0.dtype);
+  const bool dev_res = device_resident(r0);
   const size_t k = b->reqs.size();
+  if (dev_res && k == 1) return launch_direct(srv, b, temp_bytes);
+  const size_t es = elem_size(r0.dtype);
   size_t n = 0;
   for (auto &r : b->reqs) n += r->r.n;
-  // Layout of the batch allocation: keys/input | values or output | offsets | temp
   const size_t a_keys = 0;
   const size_t a_second = align256(n * es);
   const size_t second_bytes = r0.kind == BCX_REQ_SORT_PAIRS ? n * r0.value_bytes
                               : r0.kind == BCX_REQ_EXCLUSIVE_SCAN ? n * es
                                                                    : k * es;
-  const size_t a_offs = a_second + align256(second_bytes);
-  const size_t a_temp = a_offs + align256((k + 1) * sizeof(uint64_t));
-  const size_t total = a_temp + temp_bytes;
-  BCX_CUDA(cudaMallocAsync(&b->dev, total, s));
-  char *base = static_cast<char *>(b->dev);
-  // inputs
-  size_t off = 0;
+  const size_t a_meta = a_second + align256(second_bytes);
+  char *base = nullptr;  // known after the allocation; pieces are built relative to 0 first
+  // Offsets and (device-resident) pieces, relative to the batch allocation.
   std::vector<uint64_t> offsets(k + 1, 0);
+  std::vector<CopyChunk> gather, scatter;
+  size_t off = 0;
   for (size_t i = 0; i < k; ++i) {
     const bcx_request &r = b->reqs[i]->r;
     offsets[i] = off;
-    if (r.n) {
-      BCX_CUDA(cudaMemcpyAsync(base + a_keys + off * es, r.keys, r.n * es, cudaMemcpyDefault, s));
-      if (r.kind == BCX_REQ_SORT_PAIRS && r.value_bytes)
-        BCX_CUDA(cudaMemcpyAsync(base + a_second + off * r.value_bytes, r.values, r.n * r.value_bytes,
-                                 cudaMemcpyDefault, s));
+    if (dev_res) {
+      add_pieces(gather, r.keys, reinterpret_cast<void *>(a_keys + off * es), r.n * es);
+      if (r.kind == BCX_REQ_SORT_PAIRS) {
+        add_pieces(gather, r.values, reinterpret_cast<void *>(a_second + off * r.value_bytes), r.n * r.value_bytes);
+        add_pieces(scatter, reinterpret_cast<void *>(a_keys + off * es), r.out, r.n * es);
+        add_pieces(scatter, reinterpret_cast<void *>(a_second + off * r.value_bytes), r.out_values,
+                   r.n * r.value_bytes);
+      } else if (r.kind == BCX_REQ_EXCLUSIVE_SCAN) {
+        add_pieces(scatter, reinterpret_cast<void *>(a_second + off * es), r.out, r.n * es);
+      } else {
+        add_pieces(scatter, reinterpret_cast<void *>(a_second + i * es), r.out, es);
+      }
     }
     off += r.n;
   }
   offsets[k] = off;
-  // The offsets come from a host vector that dies with this function: stage
-  // them through pageable-memory semantics (cudaMemcpyAsync from pageable
-  // memory returns once the source has been consumed).
-  BCX_CUDA(cudaMemcpyAsync(base + a_offs, offsets.data(), (k + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-  const uint64_t *d_offs = reinterpret_cast<const uint64_t *>(base + a_offs);
-  // A NULL temp with a size pointer would be a size query: pass no pointer
-  // when the call needs no temporary storage.
-  void *tmp = temp_bytes ? base + a_temp : nullptr;
-  size_t tb_val = temp_bytes;
-  size_t *tbp = temp_bytes ? &tb_val : nullptr;
-  bcx_status rc = BCX_SUCCESS;
-  const int comp = (r0.dtype == BCX_FLOAT || r0.dtype == BCX_DOUBLE) ? 1 : 0;
-  if (r0.kind == BCX_REQ_SORT_PAIRS) {
-    if (k == 1)
-      rc = r0.value_bytes ? bcx_sort_pairs(s, r0.dtype, r0.value_bytes, base + a_keys, base + a_second, n, 0, tmp, tbp)
-                          : bcx_sort_keys(s, r0.dtype, base + a_keys, n, 0, tmp, tbp);
-    else
-      rc = bcx_segmented_sort_pairs(s, r0.dtype, r0.value_bytes, base + a_keys, base + a_second, n, d_offs, k, 0,
-                                    tmp, tbp);
-  } else if (r0.kind == BCX_REQ_EXCLUSIVE_SCAN) {
-    unsigned char zero[8] = {0};
-    if (k == 1)
-      rc = bcx_scan(s, r0.dtype, BCX_PLUS, 1, zero, base + a_keys, base + a_second, n, comp, tmp, tbp);
-    else
-      rc = bcx_segmented_scan(s, r0.dtype, BCX_PLUS, 1, zero, base + a_keys, base + a_second, n, d_offs, k, comp,
-                              tmp, tbp);
+  const size_t offs_bytes = align256((k + 1) * sizeof(uint64_t));
+  const size_t meta_bytes = offs_bytes + (gather.size() + scatter.size()) * sizeof(CopyChunk);
+  const size_t a_temp = a_meta + align256(meta_bytes);
+  const size_t total = a_temp + temp_bytes;
+  if (slot.stage_bytes < meta_bytes) {
+    if (slot.stage) BCX_CUDA(cudaFreeHost(slot.stage));
+    slot.stage = nullptr;
+    slot.stage_bytes = 0;
+    const size_t want = std::max(meta_bytes, size_t(1) << 20);
+    BCX_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&slot.stage), want, cudaHostAllocDefault));
+    slot.stage_bytes = want;
+  }
+  BCX_CUDA(cudaMallocAsync(&b->dev, total, s));
+  base = static_cast<char *>(b->dev);
+  // Rebase the batch-relative addresses of the pieces.
+  for (auto &c : gather) c.dst = base + reinterpret_cast<uintptr_t>(c.dst);
+  for (auto &c : scatter) c.src = base + reinterpret_cast<uintptr_t>(c.src);
+  std::memcpy(slot.stage, offsets.data(), (k + 1) * sizeof(uint64_t));
+  CopyChunk *stage_pieces = reinterpret_cast<CopyChunk *>(slot.stage + offs_bytes);
+  if (!gather.empty()) std::memcpy(stage_pieces, gather.data(), gather.size() * sizeof(CopyChunk));
+  if (!scatter.empty())
+    std::memcpy(stage_pieces + gather.size(), scatter.data(), scatter.size() * sizeof(CopyChunk));
+  BCX_CUDA(cudaMemcpyAsync(base + a_meta, slot.stage, meta_bytes, cudaMemcpyHostToDevice, s));
+  const uint64_t *d_offs = reinterpret_cast<const uint64_t *>(base + a_meta);
+  const CopyChunk *d_pieces = reinterpret_cast<const CopyChunk *>(base + a_meta + offs_bytes);
+  // inputs
+  if (dev_res) {
+    bcx_status rc = copy_chunks(d_pieces, gather.size(), s);
+    if (rc) return rc;
   } else {
-    unsigned char zero[8] = {0};
-    if (k == 1)
-      rc = bcx_reduce(s, r0.dtype, BCX_PLUS, base + a_keys, n, base + a_second, comp, tmp, tbp);
-    else
-      rc = bcx_segmented_reduce(s, r0.dtype, BCX_PLUS, base + a_keys, d_offs, k, zero, base + a_second, comp, tmp,
-                                tbp);
-  }
-  if (rc) {
-    for (auto &r : b->reqs) r->status = rc;
-  }
-  // outputs
-  off = 0;
-  for (size_t i = 0; i < k; ++i) {
-    const bcx_request &r = b->reqs[i]->r;
-    if (r.kind == BCX_REQ_SORT_PAIRS) {
+    off = 0;
+    for (size_t i = 0; i < k; ++i) {
+      const bcx_request &r = b->reqs[i]->r;
       if (r.n) {
-        BCX_CUDA(cudaMemcpyAsync(r.out, base + a_keys + off * es, r.n * es, cudaMemcpyDefault, s));
-        if (r.value_bytes)
-          BCX_CUDA(cudaMemcpyAsync(r.out_values, base + a_second + off * r.value_bytes, r.n * r.value_bytes,
+        BCX_CUDA(cudaMemcpyAsync(base + a_keys + off * es, r.keys, r.n * es, cudaMemcpyDefault, s));
+        if (r.kind == BCX_REQ_SORT_PAIRS && r.value_bytes)
+          BCX_CUDA(cudaMemcpyAsync(base + a_second + off * r.value_bytes, r.values, r.n * r.value_bytes,
                                    cudaMemcpyDefault, s));
       }
-    } else if (r.kind == BCX_REQ_EXCLUSIVE_SCAN) {
-      if (r.n) BCX_CUDA(cudaMemcpyAsync(r.out, base + a_second + off * es, r.n * es, cudaMemcpyDefault, s));
-    } else {
-      BCX_CUDA(cudaMemcpyAsync(r.out, base + a_second + i * es, es, cudaMemcpyDefault, s));
+      off += r.n;
     }
-    off += r.n;
+  }
+  bcx_status rc = run_op(r0, s, k, n, base + a_keys, base + a_second, d_offs, base + a_temp, temp_bytes);
+  if (rc)
+    for (auto &r : b->reqs) r->status = rc;
+  // outputs
+  if (dev_res) {
+    bcx_status rc2 = copy_chunks(d_pieces + gather.size(), scatter.size(), s);
+    if (rc2) return rc2;
+  } else {
+    off = 0;
+    for (size_t i = 0; i < k; ++i) {
+      const bcx_request &r = b->reqs[i]->r;
+      if (r.kind == BCX_REQ_SORT_PAIRS) {
+        if (r.n) {
+          BCX_CUDA(cudaMemcpyAsync(r.out, base + a_keys + off * es, r.n * es, cudaMemcpyDefault, s));
+          if (r.value_bytes)
+            BCX_CUDA(cudaMemcpyAsync(r.out_values, base + a_second + off * r.value_bytes, r.n * r.value_bytes,
+                                     cudaMemcpyDefault, s));
+        }
+      } else if (r.kind == BCX_REQ_EXCLUSIVE_SCAN) {
+        if (r.n) BCX_CUDA(cudaMemcpyAsync(r.out, base + a_second + off * es, r.n * es, cudaMemcpyDefault, s));
+      } else {
+        BCX_CUDA(cudaMemcpyAsync(r.out, base + a_second + i * es, es, cudaMemcpyDefault, s));
+      }
+      off += r.n;
+    }
   }
   BCX_CUDA(cudaFreeAsync(b->dev, s));
   BCX_CUDA(cudaLaunchHostFunc(s, on_batch_done, b));
@@ -250,7 +340,8 @@ size_t batch_temp(const std::vector<std::shared_ptr<Request>> &reqs, size_t n) {
 }
 
 bool same_group(const bcx_request &a, const bcx_request &b) {
-  return a.kind == b.kind && a.dtype == b.dtype && a.value_bytes == b.value_bytes;
+  return a.kind == b.kind && a.dtype == b.dtype && a.value_bytes == b.value_bytes &&
+         device_resident(a) == device_resident(b);
 }
 
 void scheduler_loop(bcx_server *srv) {
@@ -287,9 +378,16 @@ void scheduler_loop(bcx_server *srv) {
       }
     }
     size_t bytes = 0;
-    for (auto &r : reqs) bytes += request_bytes(r->r);
     const size_t temp = batch_temp(reqs, n);
-    bytes += temp + 2 * 256 + align256((reqs.size() + 1) * 8);
+    if (reqs.size() == 1 && device_resident(first->r)) {
+      bytes = temp;  // computes on the caller's buffers
+    } else {
+      for (auto &r : reqs) bytes += request_bytes(r->r);
+      // offsets and copy pieces: at most 4 buffers per request, one piece per
+      // started kCopyChunkBytes of each
+      const size_t pieces = 4 * reqs.size() + 2 * bytes / kCopyChunkBytes;
+      bytes += temp + 3 * 256 + align256((reqs.size() + 1) * 8) + pieces * sizeof(CopyChunk);
+    }
     if (srv->used + bytes > srv->budget && srv->used > 0) {
       // Not enough memory right now: wait for a completion to free some.
       srv->cv.wait(lk);
@@ -449,7 +547,10 @@ bcx_status bcx_server_destroy(bcx_server *srv) {
   }
   srv->cv.notify_all();
   if (srv->scheduler.joinable()) srv->scheduler.join();
-  for (auto &sl : srv->slots) cudaStreamDestroy(sl.stream);
+  for (auto &sl : srv->slots) {
+    cudaStreamDestroy(sl.stream);
+    if (sl.stage) cudaFreeHost(sl.stage);
+  }
   delete srv;
   return BCX_SUCCESS;
 }

@@ -190,7 +190,41 @@ bcx_status binary_int_t(cudaStream_t s, int op, const void *a, const void *b, vo
   return binary_common_t<T>(s, op, a, b, out, n);
 }
 
+// One block per piece.  Pieces whose ends are 16-byte aligned move in 16-byte
+// vectors; 4-byte aligned pieces (a request's elements packed at an arbitrary
+// element offset of a batch) in words; anything else in bytes.
+__global__ void __launch_bounds__(256) copy_chunks_kernel(const CopyChunk *__restrict__ chunks) {
+  const CopyChunk c = chunks[blockIdx.x];
+  const uintptr_t a = reinterpret_cast<uintptr_t>(c.src) | reinterpret_cast<uintptr_t>(c.dst) | c.bytes;
+  if ((a & 15) == 0) {
+    const uint4 *src = static_cast<const uint4 *>(c.src);
+    uint4 *dst = static_cast<uint4 *>(c.dst);
+    const uint32_t n = uint32_t(c.bytes >> 4);
+#pragma unroll 4
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  } else if ((a & 3) == 0) {
+    const uint32_t *src = static_cast<const uint32_t *>(c.src);
+    uint32_t *dst = static_cast<uint32_t *>(c.dst);
+    const uint32_t n = uint32_t(c.bytes >> 2);
+#pragma unroll 4
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  } else {
+    const unsigned char *src = static_cast<const unsigned char *>(c.src);
+    unsigned char *dst = static_cast<unsigned char *>(c.dst);
+    for (uint32_t i = threadIdx.x; i < c.bytes; i += blockDim.x) dst[i] = src[i];
+  }
+}
+
 }  // namespace
+
+bcx_status copy_chunks(const CopyChunk *chunks, size_t count, cudaStream_t s) {
+  if (count == 0) return BCX_SUCCESS;
+  BCX_CHECK(count <= 0x7fffffffu, BCX_INVALID_VALUE, "too many copy pieces");
+  KernelScope ks("copy_chunks", s);
+  copy_chunks_kernel<<<unsigned(count), 256, 0, s>>>(chunks);
+  return launch_status("copy_chunks");
+}
+
 }  // namespace bcx
 
 using namespace bcx;

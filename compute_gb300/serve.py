@@ -47,6 +47,12 @@ class Server:
         self._keep[t.value] = (keys, values, out, out_values)
         return t.value
 
+    def submit_request(self, req: Request) -> int:
+        """Queue a prepared bcx_request; its buffers are the caller's to keep alive."""
+        t = C.c_uint64(0)
+        check(lib().bcx_server_submit(self._h, C.byref(req), C.byref(t)), "server_submit")
+        return t.value
+
     def wait(self, ticket: int) -> float:
         ms = C.c_double(0)
         try:

@@ -313,6 +313,39 @@ bcx_status bcx_jit_cache_configure(size_t capacity, int clear);
  * kernels). */
 bcx_status bcx_device_sm_count(int *sm_count);
 
+/* ---- tuning parameters and autotuner (detail::parameter_cache,
+ *      detail/parameter_cache.hpp:38-110; the perf/ tuning programs that fill
+ *      it) ---------------------------------------------------------------
+ * A per-device table (object, parameter) -> unsigned, kept in memory and, when
+ * BCX_CACHE_DIR is set, in $BCX_CACHE_DIR/tune/<device name>.json (read on
+ * first use, written by bcx_param_save and by every tuner).  Tunables read at
+ * dispatch time:
+ *   "segmented_sort_k<key bits>_v<value bytes>": "small_tile" (1024, 2048 or
+ *       4096: segments up to this many pairs sort in shared memory),
+ *       "small_blocks_per_sm" (0 = as many as fit);
+ *   "segmented_scan_<type>": "items_per_thread" (8/16 for 4-byte types, 4/8
+ *       for 8-byte types);
+ *   "segmented_reduce_<type>": "blocks_per_sm".
+ * Temporary-storage sizes never depend on these values. */
+bcx_status bcx_param_get(const char *object, const char *parameter, unsigned default_value, unsigned *value);
+bcx_status bcx_param_set(const char *object, const char *parameter, unsigned value);
+bcx_status bcx_param_save(void);
+/* Forgets the in-memory tables (the next lookup re-reads the file). */
+bcx_status bcx_param_clear(void);
+/* Autotuners: time every candidate value of the operation's tunables on the
+ * caller's workload (CUDA events, median of 3 runs after a warm-up; inputs are
+ * left unchanged -- trial runs sort copies and write scratch outputs), store
+ * the fastest and save the table.  `report` (optional) receives one line per
+ * trial: "<object>.<parameter>=<value> <ms> ms".  They synchronize the
+ * stream and allocate scratch memory: not for use inside stream capture. */
+bcx_status bcx_tune_segmented_sort_pairs(bcx_stream stream, bcx_dtype key_type, size_t value_bytes,
+                                         const void *keys, const void *values, size_t n, const uint64_t *offsets,
+                                         size_t nseg, char *report, size_t report_len);
+bcx_status bcx_tune_segmented_scan(bcx_stream stream, bcx_dtype type, const void *in, size_t n,
+                                   const uint64_t *offsets, size_t nseg, char *report, size_t report_len);
+bcx_status bcx_tune_segmented_reduce(bcx_stream stream, bcx_dtype type, const void *in, const uint64_t *offsets,
+                                     size_t nseg, char *report, size_t report_len);
+
 /* ---- profiling (command_queue::enable_profiling / event::duration,
  *      command_queue.hpp:82, event.hpp:269) --------------------------------
  * When enabled, every kernel this library launches is bracketed by CUDA

@@ -7,4 +7,5 @@
 #include <boost/compute/algorithm/scan.hpp>
 #include <boost/compute/algorithm/sort.hpp>
 #include <boost/compute/algorithm/transform.hpp>
+#include <boost/compute/algorithm/transform_reduce.hpp>
 #endif

@@ -150,15 +150,22 @@ inline void jit_transform(const std::string &defs, const std::string &expr, cons
   jit_launch(src.str(), "bcx_jit_transform", grid_for(n / 4 + 1, 256), 256, queue, args);
 }
 
-// result = init OP fold(in) (has_init) or fold(in); one value of type T at
-// `out` (device).  OP is an expression of (_1, _2).
-inline void jit_reduce(const std::string &defs, const std::string &op, const char *t, size_t tsize,
-                       const void *in, size_t n, const void *init, void *out, command_queue &queue) {
-  (void)tsize;
+// result = init OP fold(load(i)) (has_init) or fold(load(i)); one value of
+// type T at `out` (device).  OP is an expression of (_1, _2); LOAD the body of
+// the element read, a function of a[i] (and b[i]) -- "return a[i];" for a
+// plain reduce, the transform function applied to a[i] (and b[i]) for a fused
+// transform_reduce, so the transformed values are never written out.
+inline void jit_fold(const std::string &defs, const std::string &op, const char *t, size_t tsize,
+                     const std::string &load, const char *ta, const char *tb, const void *a, const void *b,
+                     size_t n, const void *init, void *out, command_queue &queue) {
   std::ostringstream src;
   src << jit_prelude() << defs << "\n"
       << "typedef " << t << " T;\n"
+      << "typedef " << ta << " TA;\n"
+      << "typedef " << (tb ? tb : ta) << " TB;\n"
       << "__device__ __forceinline__ T bcx_op(const T &_1, const T &_2) { return (T)(" << op << "); }\n"
+      << "__device__ __forceinline__ T bcx_load(const TA *__restrict__ a, const TB *__restrict__ b,"
+      << " unsigned long long i) { " << load << " }\n"
       << "struct Acc { T v; int has; };\n"
       << "__device__ __forceinline__ Acc comb(Acc a, Acc b) {\n"
       << "  if (!a.has) return b; if (!b.has) return a; Acc r; r.v = bcx_op(a.v, b.v); r.has = 1; return r; }\n"
@@ -171,22 +178,23 @@ inline void jit_reduce(const std::string &defs, const std::string &op, const cha
       << "      Acc z = comb(x, y); sv[threadIdx.x] = z.v; sh[threadIdx.x] = z.has; }\n"
       << "    __syncthreads(); }\n"
       << "  Acc r{sv[0], sh[0]}; return r; }\n"
-      << "extern \"C\" __global__ void bcx_jit_reduce_partials(const T *__restrict__ in, unsigned long long n,"
-      << " T *__restrict__ pv, int *__restrict__ ph) {\n"
+      << "extern \"C\" __global__ void bcx_jit_reduce_partials(const TA *__restrict__ a, const TB *__restrict__ b,"
+      << " unsigned long long n, T *__restrict__ pv, int *__restrict__ ph) {\n"
       << "  const unsigned long long per = (n + gridDim.x - 1) / gridDim.x;\n"
       << "  const unsigned long long b0 = blockIdx.x * per, b1 = b0 + per < n ? b0 + per : n;\n"
-      << "  Acc a; a.has = 0; a.v = T();\n"
+      << "  Acc acc; acc.has = 0; acc.v = T();\n"
       << "  const unsigned long long chunk = (b1 > b0 ? b1 - b0 : 0) / blockDim.x + 1;\n"
       << "  const unsigned long long t0 = b0 + threadIdx.x * chunk;\n"
-      << "  for (unsigned long long i = t0; i < t0 + chunk && i < b1; ++i) { Acc x; x.v = in[i]; x.has = 1; a = comb(a, x); }\n"
-      << "  a = block_fold(a);\n"
-      << "  if (threadIdx.x == 0) { pv[blockIdx.x] = a.v; ph[blockIdx.x] = a.has; } }\n"
+      << "  for (unsigned long long i = t0; i < t0 + chunk && i < b1; ++i) {"
+      << " Acc x; x.v = bcx_load(a, b, i); x.has = 1; acc = comb(acc, x); }\n"
+      << "  acc = block_fold(acc);\n"
+      << "  if (threadIdx.x == 0) { pv[blockIdx.x] = acc.v; ph[blockIdx.x] = acc.has; } }\n"
       << "extern \"C\" __global__ void bcx_jit_reduce_final(const T *__restrict__ pv, const int *__restrict__ ph,"
       << " int count, const T *__restrict__ init, T *__restrict__ out) {\n"
       << "  if (threadIdx.x != 0) return;\n"
-      << "  Acc a; a.has = init != 0; a.v = init ? *init : T();\n"
-      << "  for (int i = 0; i < count; ++i) { Acc x{pv[i], ph[i]}; a = comb(a, x); }\n"
-      << "  if (a.has) *out = a.v; }\n";
+      << "  Acc acc; acc.has = init != 0; acc.v = init ? *init : T();\n"
+      << "  for (int i = 0; i < count; ++i) { Acc x{pv[i], ph[i]}; acc = comb(acc, x); }\n"
+      << "  if (acc.has) *out = acc.v; }\n";
   const std::string s = src.str();
   // Each thread folds a contiguous run in index order and the block folds
   // threads in order, so non-commutative (but associative) functors work.
@@ -199,7 +207,8 @@ inline void jit_reduce(const std::string &defs, const std::string &op, const cha
     check(bcx_memcpy_async(dinit, init, tsize, queue.get()));
   }
   unsigned long long nn = n;
-  void *a1[] = {(void *)&in, (void *)&nn, (void *)&partials, (void *)&flags};
+  const void *bb = b ? b : a;
+  void *a1[] = {(void *)&a, (void *)&bb, (void *)&nn, (void *)&partials, (void *)&flags};
   jit_launch(s, "bcx_jit_reduce_partials", blocks, 256, queue, a1);
   int count = int(blocks);
   void *a2[] = {(void *)&partials, (void *)&flags, (void *)&count, (void *)&dinit, (void *)&out};
@@ -208,6 +217,11 @@ inline void jit_reduce(const std::string &defs, const std::string &op, const cha
   bcx_free(partials);
   bcx_free(flags);
   if (dinit) bcx_free(dinit);
+}
+
+inline void jit_reduce(const std::string &defs, const std::string &op, const char *t, size_t tsize,
+                       const void *in, size_t n, const void *init, void *out, command_queue &queue) {
+  jit_fold(defs, op, t, tsize, "return a[i];", t, nullptr, in, nullptr, n, init, out, queue);
 }
 
 // Scan with a user functor: tile totals -> one block scans them -> tiles

@@ -243,6 +243,44 @@ static void jit_cases(compute::command_queue &q) {
   CHECK(threw);
 }
 
+static void transform_reduce_cases(compute::command_queue &q) {
+  using compute::_1;
+  using compute::_2;
+  // test/test_transform_reduce.cpp:27-45 (sum of absolute values)
+  int ad[] = {1, -2, 3, -4, 5};
+  compute::vector<int> av(ad, ad + 5, q);
+  int sum = 0;
+  compute::transform_reduce(av.begin(), av.end(), &sum, compute::abs<int>(), compute::plus<int>(), q);
+  CHECK(sum == 15);
+  // lambda transform, device result
+  float fd[] = {1.f, 2.f, 3.f, 4.f};
+  compute::vector<float> fv(fd, fd + 4, q), fr(1, q.get_context());
+  compute::transform_reduce(fv.begin(), fv.end(), fr.begin(), _1 * _1, compute::plus<float>(), q);
+  CHECK(fr.begin().read(q) == 30.f);
+  // binary form: dot product of 2^20 + 7 integers (exact, wraps mod 2^32)
+  const size_t n = (1 << 20) + 7;
+  std::vector<int> ha(n), hb(n);
+  unsigned long long expect = 0;
+  for (size_t i = 0; i < n; ++i) {
+    ha[i] = int(i % 1000) - 500;
+    hb[i] = int((i * 7) % 300);
+    expect += (unsigned long long)(long long)(ha[i] * hb[i]);
+  }
+  compute::vector<int> a(ha.begin(), ha.end(), q), b(hb.begin(), hb.end(), q);
+  int dot = 0;
+  compute::transform_reduce(a.begin(), a.end(), b.begin(), &dot, compute::multiplies<int>(), compute::plus<int>(), q);
+  CHECK(dot == int(unsigned(expect)));
+  // user function transform, built-in max reduce
+  BOOST_COMPUTE_FUNCTION(int, sq_minus, (int x), { return x * x - 10; });
+  int mx = 0;
+  compute::transform_reduce(av.begin(), av.end(), &mx, sq_minus, compute::max<int>(), q);
+  CHECK(mx == 15);
+  // binary lambda transform, lambda reduce
+  compute::vector<int> r1(1, q.get_context());
+  compute::transform_reduce(a.begin(), a.begin() + 4, b.begin(), r1.begin(), _1 - _2, _1 + _2, q);
+  CHECK(r1.begin().read(q) == (-500 - 0) + (-499 - 7) + (-498 - 14) + (-497 - 21));
+}
+
 static void error_cases(compute::command_queue &q) {
   // bcx errors surface as opencl_error with the OpenCL status code
   bool thrown = false;
@@ -264,6 +302,7 @@ int main() {
   transform_cases(q);
   reduce_by_key_cases(q);
   jit_cases(q);
+  transform_reduce_cases(q);
   error_cases(q);
   q.check_device_errors();
   std::printf("%s (%d failures)\n", g_failures ? "FAILED" : "OK", g_failures);

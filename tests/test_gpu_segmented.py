@@ -149,3 +149,92 @@ def test_segmented_sort_keys_only_and_8bit(cuda):
     for s in range(offsets.size - 1):
         a, b = int(offsets[s]), int(offsets[s + 1])
         np.testing.assert_array_equal(gk[a:b], np.sort(keys[a:b], kind="stable"))
+
+
+def _set_param(obj, param, value):
+    from compute_gb300 import _lib
+    assert _lib.lib().bcx_param_set(obj.encode(), param.encode(), value) == 0
+
+
+@pytest.mark.parametrize("tile", [1024, 2048, 4096])
+@pytest.mark.parametrize("per_sm", [0, 1, 8])
+def test_segmented_sort_every_small_tile(cuda, tile, per_sm):
+    """Every compiled shared-memory tile and grid the autotuner may choose gives
+    the same stable per-segment order (segments straddle each tile size)."""
+    rng = np.random.default_rng(tile + per_sm)
+    offsets = log_uniform_offsets(rng, 400, 1, 12_000)
+    n = int(offsets[-1])
+    keys = rng.integers(0, 1 << 12, size=n).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    _set_param("segmented_sort_k32_v4", "small_tile", tile)
+    _set_param("segmented_sort_k32_v4", "small_blocks_per_sm", per_sm)
+    try:
+        gk, gv = run_seg_sort(cuda, keys, vals, "uint", offsets)
+    finally:
+        from compute_gb300 import _lib
+        _lib.lib().bcx_param_clear()
+    for s in range(offsets.size - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        rk, rv = oracle.radix_sort(keys[a:b], "uint", values=vals[a:b])
+        np.testing.assert_array_equal(gk[a:b], rk, err_msg=f"keys seg {s}")
+        np.testing.assert_array_equal(gv[a:b], rv, err_msg=f"values seg {s}")
+
+
+@pytest.mark.parametrize("dtype,items", [("int", 16), ("int", 8), ("long", 4), ("float", 16)])
+def test_segmented_scan_every_tile(cuda, dtype, items):
+    rng = np.random.default_rng(items)
+    offsets = log_uniform_offsets(rng, 500, 1, 30_000, empty_frac=0.05)
+    n = int(offsets[-1])
+    x = rng.integers(-100, 100, size=n).astype(NP[dtype])
+    _set_param(f"segmented_scan_{dtype}", "items_per_thread", items)
+    try:
+        got = run_seg_scan(cuda, x, dtype, "plus", True, 3, offsets)
+    finally:
+        from compute_gb300 import _lib
+        _lib.lib().bcx_param_clear()
+    for s in range(offsets.size - 1):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        if a < b:
+            np.testing.assert_array_equal(got[a:b], oracle.scan(x[a:b], dtype, exclusive=True, init=3))
+
+
+def test_autotuner_records_fastest(cuda, tmp_path, monkeypatch):
+    """The tuners time each candidate, store one of them and write the table."""
+    from compute_gb300 import _lib
+    lib = _lib.lib()
+    monkeypatch.setenv("BCX_CACHE_DIR", str(tmp_path))
+    lib.bcx_param_clear()
+    rng = np.random.default_rng(5)
+    offsets = log_uniform_offsets(rng, 2000, 16, 1 << 14)
+    n = int(offsets[-1])
+    keys = cuda.randint(0, 2**31 - 1, (n,), dtype=cuda.int32, device="cuda")
+    before = keys.clone()
+    vals = cuda.arange(n, dtype=cuda.int32, device="cuda")
+    offs = cuda.from_numpy(offsets.view(np.int64).copy()).cuda()
+    s = cuda.cuda.current_stream().cuda_stream
+    buf = ctypes.create_string_buffer(8192)
+    try:
+        rc = lib.bcx_tune_segmented_sort_pairs(s, _lib.DTYPES["uint"], 4, keys.data_ptr(), vals.data_ptr(), n,
+                                               offs.data_ptr(), offsets.size - 1, buf, len(buf))
+        assert rc == 0, lib.bcx_last_error_string()
+        report = buf.value.decode()
+        assert "segmented_sort_k32_v4.small_tile=1024" in report and "-> " in report
+        rc = lib.bcx_tune_segmented_scan(s, _lib.DTYPES["int"], keys.data_ptr(), n, offs.data_ptr(),
+                                         offsets.size - 1, buf, len(buf))
+        assert rc == 0, lib.bcx_last_error_string()
+        rc = lib.bcx_tune_segmented_reduce(s, _lib.DTYPES["int"], keys.data_ptr(), offs.data_ptr(),
+                                           offsets.size - 1, buf, len(buf))
+        assert rc == 0, lib.bcx_last_error_string()
+        assert cuda.equal(keys, before)  # trial runs worked on copies
+        files = list((tmp_path / "tune").glob("*.json"))
+        assert len(files) == 1
+        text = files[0].read_text()
+        for key in ("segmented_sort_k32_v4", "small_tile", "segmented_scan_int", "segmented_reduce_int"):
+            assert key in text
+        v = ctypes.c_uint(0)
+        lib.bcx_param_clear()  # re-read from the file
+        assert lib.bcx_param_get(b"segmented_sort_k32_v4", b"small_tile", 7, ctypes.byref(v)) == 0
+        assert v.value in (1024, 2048, 4096)
+    finally:
+        monkeypatch.delenv("BCX_CACHE_DIR")
+        lib.bcx_param_clear()

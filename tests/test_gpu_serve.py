@@ -69,9 +69,12 @@ def test_server_results_match_alone(cuda):
                 assert out[0] == oracle.fold(keys, dtype)
 
 
-def test_server_device_resident_out_of_place(cuda):
+@pytest.mark.parametrize("small_limit", [None, 0], ids=["batched", "direct"])
+def test_server_device_resident_out_of_place(cuda, small_limit):
     """Device buffers, sorts written out of place: inputs are left untouched and
-    several requests may read the same input buffer."""
+    several requests may read the same input buffer.  Batched requests move
+    through one gather and one scatter launch; with small_limit=0 every
+    request computes directly on its own buffers."""
     import torch
     from compute_gb300.serve import Server
     rng = np.random.default_rng(7)
@@ -79,7 +82,8 @@ def test_server_device_resident_out_of_place(cuda):
     dk = torch.from_numpy(shared.view(np.int32)).to("cuda")
     dv = torch.arange(shared.size, dtype=torch.int32, device="cuda")
     outs = []
-    with Server(slots=4) as srv:
+    red = torch.zeros(1, dtype=torch.int64, device="cuda")
+    with Server(slots=4, small_limit=small_limit) as srv:
         tickets = []
         for i in range(24):
             n = int(rng.integers(1, shared.size + 1))
@@ -90,6 +94,7 @@ def test_server_device_resident_out_of_place(cuda):
             outs.append((n, ok, ov))
         os_ = torch.empty(shared.size, dtype=torch.int32, device="cuda")
         tickets.append(srv.submit("exclusive_scan", "uint", dk, out=os_, device=True))
+        tickets.append(srv.submit("reduce", "ulong", dk, out=red, n=shared.size // 2, device=True))
         for t in tickets:
             srv.wait(t)
     assert np.array_equal(dk.cpu().numpy().view(np.uint32), shared)
@@ -98,3 +103,5 @@ def test_server_device_resident_out_of_place(cuda):
         assert np.array_equal(ok.cpu().numpy().view(np.uint32), rk)
         assert np.array_equal(ov.cpu().numpy().view(np.uint32), rv)
     assert np.array_equal(os_.cpu().numpy().view(np.uint32), oracle.scan(shared, "uint", exclusive=True))
+    as_u64 = shared.view(np.uint64)  # the same bytes read as n/2 uint64 values
+    assert int(red.cpu().numpy().view(np.uint64)[0]) == int(oracle.fold(as_u64, "ulong"))
