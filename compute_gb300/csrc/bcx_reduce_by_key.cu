@@ -255,7 +255,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
     }
     if (idx < n) {
       const uint32_t run_idx = (incl.c & kCountMask) - 1u;
-      if (h) keys_out[run_idx] = k[i];
+      if (h && keys_out) keys_out[run_idx] = k[i];
       if (idx + 1 == n || next_head) vals_out[run_idx] = P::out(incl.v);
       if (idx + 1 == n) *num_runs = (unsigned long long)(incl.c & kCountMask);
     }
@@ -349,8 +349,7 @@ extern "C" bcx_status bcx_reduce_by_key(bcx_stream stream, bcx_dtype key_type, b
     if (num_runs_dev) BCX_CUDA(cudaMemsetAsync(num_runs_dev, 0, sizeof(uint64_t), s));
     return BCX_SUCCESS;
   }
-  BCX_CHECK(keys_in && values_in && keys_out && values_out && num_runs_dev, BCX_INVALID_VALUE,
-            "NULL argument");
+  BCX_CHECK(keys_in && values_in && values_out && num_runs_dev, BCX_INVALID_VALUE, "NULL argument");
   bcx_status rc = BCX_UNSUPPORTED;
   switch (key_type) {
     case BCX_INT: rc = rbk_val<int32_t>(s, value_type, op, compensated, keys_in, values_in, n, keys_out, values_out, num_runs_dev, temp, temp_bytes); break;

@@ -204,7 +204,9 @@ bcx_status bcx_transform_saxpy(bcx_stream stream, bcx_dtype type, const void *al
  * per run of equal consecutive keys; the run count goes to *num_runs_dev
  * (a device uint64).  Key types int/uint/long/ulong/float (typed ==);
  * value types int/uint/long/ulong/float/double; functors plus, multiplies,
- * min, max.  compensated = 1 with float plus keeps Neumaier pairs. */
+ * min, max.  compensated = 1 with float plus keeps Neumaier pairs.
+ * keys_out may be NULL (the run keys are discarded, as with a
+ * discard_iterator output). */
 bcx_status bcx_reduce_by_key(bcx_stream stream, bcx_dtype key_type,
                              bcx_dtype value_type, bcx_op op,
                              const void *keys_in, const void *values_in, size_t n,

@@ -8,6 +8,7 @@
 #include <boost/compute/functional.hpp>
 #include <boost/compute/iterator/buffer_iterator.hpp>
 #include <boost/compute/iterator/counting_iterator.hpp>
+#include <boost/compute/iterator/discard_iterator.hpp>
 #include <boost/compute/iterator/transform_iterator.hpp>
 #include <boost/compute/function.hpp>
 #include <boost/compute/lambda.hpp>

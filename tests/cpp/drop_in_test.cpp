@@ -169,6 +169,13 @@ static void reduce_by_key_cases(compute::command_queue &q) {
   std::vector<int> hk = to_host(ko, q), hv = to_host(vo, q);
   CHECK((std::vector<int>(hk.begin(), hk.begin() + 4) == std::vector<int>{0, 2, -3, 4}));
   CHECK((std::vector<int>(hv.begin(), hv.begin() + 4) == std::vector<int>{1, 1, 10, 1}));
+  // run keys discarded
+  compute::vector<int> vo2(8, q.get_context());
+  auto ends2 = compute::reduce_by_key(ki.begin(), ki.end(), vi.begin(), compute::make_discard_iterator(),
+                                      vo2.begin(), compute::plus<int>(), q);
+  CHECK(ends2.first.get_index() == 4 && ends2.second - vo2.begin() == 4);
+  std::vector<int> hv2 = to_host(vo2, q);
+  CHECK((std::vector<int>(hv2.begin(), hv2.begin() + 4) == std::vector<int>{1, 1, 10, 1}));
 }
 
 static void jit_cases(compute::command_queue &q) {
