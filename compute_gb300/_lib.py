@@ -73,6 +73,7 @@ SIGNATURES = {
     "bcx_server_configure": (_i, [_vp, _sz, _sz, _sz]),
     "bcx_server_submit": (_i, [_vp, C.c_void_p, C.POINTER(C.c_uint64)]),
     "bcx_server_wait": (_i, [_vp, C.c_uint64, C.POINTER(C.c_double)]),
+    "bcx_server_wait_for": (_i, [_vp, C.c_uint64, C.c_double, C.POINTER(C.c_double)]),
     "bcx_server_drain": (_i, [_vp]),
     "bcx_server_stats": (_i, [_vp, C.c_void_p]),
     "bcx_server_reset_stats": (_i, [_vp]),

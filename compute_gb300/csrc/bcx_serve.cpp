@@ -193,8 +193,8 @@ void add_pieces(std::vector<CopyChunk> &v, const void *src, void *dst, size_t by
                           uint64_t(std::min(kCopyChunkBytes, bytes - o)), 0});
 }
 
-// Enqueue one batch on its slot stream.  Called with the server lock held
-// (only enqueues asynchronous work).  Layout of the batch allocation:
+// Enqueue one batch on its slot stream.  Called without the server lock.
+// Layout of the batch allocation:
 // keys/input | values or output | offsets + copy pieces | temp.  Host
 // buffers move with one copy per buffer; device-resident buffers move with
 // one gather launch in and one scatter launch out for the whole batch.
@@ -339,11 +339,24 @@ size_t batch_temp(const std::vector<std::shared_ptr<Request>> &reqs, size_t n) {
   return rc ? 0 : tb;
 }
 
+// No request waiting or running (server lock held).
+bool idle_locked(const bcx_server *srv) {
+  if (!srv->pending.empty()) return false;
+  for (auto &sl : srv->slots)
+    if (sl.busy) return false;
+  return true;
+}
+
 bool same_group(const bcx_request &a, const bcx_request &b) {
   return a.kind == b.kind && a.dtype == b.dtype && a.value_bytes == b.value_bytes &&
          device_resident(a) == device_resident(b);
 }
 
+// The scheduler never holds the server lock across a CUDA call: batch
+// completions run as host functions on CUDA's callback thread and take the
+// lock, and a CUDA call that waits for stream progress (a copy from pageable
+// memory, first-use device setup) would otherwise wait for a callback that
+// waits for the lock.
 void scheduler_loop(bcx_server *srv) {
   cudaSetDevice(srv->device);
   std::unique_lock<std::mutex> lk(srv->mu);
@@ -363,7 +376,8 @@ void scheduler_loop(bcx_server *srv) {
         break;
       }
     if (slot < 0 || srv->pending.empty()) continue;
-    // Build a batch around the oldest request.
+    // Build a batch around the oldest request (only this thread removes
+    // requests from `pending`, so the batch stays valid while unlocked).
     auto first = srv->pending.front();
     std::vector<std::shared_ptr<Request>> reqs{first};
     size_t n = first->r.n;
@@ -377,8 +391,9 @@ void scheduler_loop(bcx_server *srv) {
         n += q->r.n;
       }
     }
-    size_t bytes = 0;
+    lk.unlock();
     const size_t temp = batch_temp(reqs, n);
+    size_t bytes = 0;
     if (reqs.size() == 1 && device_resident(first->r)) {
       bytes = temp;  // computes on the caller's buffers
     } else {
@@ -388,6 +403,7 @@ void scheduler_loop(bcx_server *srv) {
       const size_t pieces = 4 * reqs.size() + 2 * bytes / kCopyChunkBytes;
       bytes += temp + 3 * 256 + align256((reqs.size() + 1) * 8) + pieces * sizeof(CopyChunk);
     }
+    lk.lock();
     if (srv->used + bytes > srv->budget && srv->used > 0) {
       // Not enough memory right now: wait for a completion to free some.
       srv->cv.wait(lk);
@@ -407,7 +423,11 @@ void scheduler_loop(bcx_server *srv) {
     srv->used += bytes;
     srv->batches += 1;
     if (reqs.size() > 1) srv->batched_requests += reqs.size();
-    bcx_status rc = launch_batch(srv, b, temp);
+    lk.unlock();
+    // On success the batch belongs to its completion callback from here on.
+    const bcx_status rc = launch_batch(srv, b, temp);
+    if (rc && b->dev) cudaFreeAsync(b->dev, srv->slots[slot].stream);
+    lk.lock();
     if (rc) {
       for (auto &r : reqs) {
         r->status = rc;
@@ -481,32 +501,33 @@ bcx_status bcx_server_submit(bcx_server *srv, const bcx_request *req, uint64_t *
   return BCX_SUCCESS;
 }
 
-bcx_status bcx_server_wait(bcx_server *srv, uint64_t ticket, double *latency_ms) {
+bcx_status bcx_server_wait_for(bcx_server *srv, uint64_t ticket, double timeout_ms, double *latency_ms) {
   BCX_CHECK(srv, BCX_INVALID_VALUE, "NULL server");
-  std::shared_ptr<Request> r;
-  {
-    std::lock_guard<std::mutex> lk(srv->mu);
-    auto it = srv->all.find(ticket);
-    BCX_CHECK(it != srv->all.end(), BCX_INVALID_VALUE, "unknown ticket %llu", (unsigned long long)ticket);
-    r = it->second;
-  }
   std::unique_lock<std::mutex> lk(srv->mu);
-  srv->cv.wait(lk, [&] { return r->done.load() != 0; });
+  auto it = srv->all.find(ticket);
+  BCX_CHECK(it != srv->all.end(), BCX_INVALID_VALUE, "unknown ticket %llu", (unsigned long long)ticket);
+  std::shared_ptr<Request> r = it->second;
+  auto ready = [&] { return r->done.load() != 0; };
+  if (timeout_ms < 0) {
+    srv->cv.wait(lk, ready);
+  } else if (!srv->cv.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
+    set_error("request %llu not finished after %.0f ms", (unsigned long long)ticket, timeout_ms);
+    return BCX_DEVICE_TIMEOUT;  // the ticket stays valid
+  }
   if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->finished - r->submitted).count();
   srv->all.erase(ticket);
   if (r->status) set_error("request %llu failed", (unsigned long long)ticket);
   return r->status;
 }
 
+bcx_status bcx_server_wait(bcx_server *srv, uint64_t ticket, double *latency_ms) {
+  return bcx_server_wait_for(srv, ticket, -1.0, latency_ms);
+}
+
 bcx_status bcx_server_drain(bcx_server *srv) {
   BCX_CHECK(srv, BCX_INVALID_VALUE, "NULL server");
   std::unique_lock<std::mutex> lk(srv->mu);
-  srv->cv.wait(lk, [&] {
-    if (!srv->pending.empty()) return false;
-    for (auto &sl : srv->slots)
-      if (sl.busy) return false;
-    return true;
-  });
+  srv->cv.wait(lk, [&] { return idle_locked(srv); });
   return BCX_SUCCESS;
 }
 
@@ -540,7 +561,16 @@ bcx_status bcx_server_reset_stats(bcx_server *srv) {
 
 bcx_status bcx_server_destroy(bcx_server *srv) {
   if (!srv) return BCX_SUCCESS;
-  bcx_server_drain(srv);
+  {
+    // Requests still running after a minute mean the GPU or a caller's
+    // buffers are stuck: report it and leave the server (and its streams)
+    // alive rather than block the caller forever.
+    std::unique_lock<std::mutex> lk(srv->mu);
+    if (!srv->cv.wait_for(lk, std::chrono::seconds(60), [&] { return idle_locked(srv); })) {
+      set_error("server destroy: requests still running after 60 s; server left alive");
+      return BCX_DEVICE_TIMEOUT;
+    }
+  }
   {
     std::lock_guard<std::mutex> lk(srv->mu);
     srv->stop = true;

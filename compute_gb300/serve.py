@@ -53,12 +53,15 @@ class Server:
         check(lib().bcx_server_submit(self._h, C.byref(req), C.byref(t)), "server_submit")
         return t.value
 
-    def wait(self, ticket: int) -> float:
+    def wait(self, ticket: int, timeout: float | None = None) -> float:
+        """Latency of the request in ms; with `timeout` (seconds) raises BcxError
+        (BCX_DEVICE_TIMEOUT) if it has not finished by then."""
         ms = C.c_double(0)
-        try:
-            check(lib().bcx_server_wait(self._h, C.c_uint64(ticket), C.byref(ms)), "server_wait")
-        finally:
+        limit = -1.0 if timeout is None else float(timeout) * 1e3
+        rc = lib().bcx_server_wait_for(self._h, C.c_uint64(ticket), limit, C.byref(ms))
+        if rc != -9001:
             self._keep.pop(ticket, None)
+        check(rc, "server_wait")
         return ms.value
 
     def drain(self) -> None:

@@ -283,11 +283,18 @@ bcx_status bcx_server_create(bcx_server **server, int slots, size_t memory_budge
 bcx_status bcx_server_configure(bcx_server *server, size_t small_limit, size_t batch_elems,
                                 size_t batch_count);
 bcx_status bcx_server_submit(bcx_server *server, const bcx_request *request, uint64_t *ticket);
-/* Blocks until the request's results are in host memory. */
+/* Blocks until the request's results are in place (host or device buffers). */
 bcx_status bcx_server_wait(bcx_server *server, uint64_t ticket, double *latency_ms);
+/* As bcx_server_wait, for at most timeout_ms milliseconds (negative: no
+ * limit); returns BCX_DEVICE_TIMEOUT when the request is still running, and
+ * the ticket stays valid. */
+bcx_status bcx_server_wait_for(bcx_server *server, uint64_t ticket, double timeout_ms, double *latency_ms);
 bcx_status bcx_server_drain(bcx_server *server);
 bcx_status bcx_server_stats(bcx_server *server, bcx_server_stats_t *stats);
 bcx_status bcx_server_reset_stats(bcx_server *server);
+/* Waits up to 60 s for queued and running requests, then stops the scheduler
+ * and frees the server; if requests are still running it returns
+ * BCX_DEVICE_TIMEOUT and leaves the server alive. */
 bcx_status bcx_server_destroy(bcx_server *server);
 
 /* ---- run-time compiled kernels ------------------------------------------

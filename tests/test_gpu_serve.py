@@ -44,7 +44,7 @@ def test_server_results_match_alone(cuda):
                 out = np.zeros(1, dtype=k.dtype)
             bufs.append((k, v, out))
             tickets.append(srv.submit(kind, dtype, k, values=v, out=out))
-        lat = [srv.wait(t) for t in tickets]
+        lat = [srv.wait(t, timeout=120) for t in tickets]
         st = srv.stats()
     assert st["completed"] == len(reqs)
     assert st["batched_requests"] > 0, st  # small requests were packed into shared launches
@@ -96,7 +96,7 @@ def test_server_device_resident_out_of_place(cuda, small_limit):
         tickets.append(srv.submit("exclusive_scan", "uint", dk, out=os_, device=True))
         tickets.append(srv.submit("reduce", "ulong", dk, out=red, n=shared.size // 2, device=True))
         for t in tickets:
-            srv.wait(t)
+            srv.wait(t, timeout=120)
     assert np.array_equal(dk.cpu().numpy().view(np.uint32), shared)
     for n, ok, ov in outs:
         rk, rv = oracle.radix_sort(shared[:n], "uint", values=np.arange(n, dtype=np.uint32))
