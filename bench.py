@@ -101,13 +101,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def dist_init(n_gpus):
+def dist_init(n_gpus, backend="nccl"):
+    """Rank, world size and local rank from the torchrun environment; joins
+    the process group when there is more than one rank (replicas: the group
+    only carries the barrier and the max-over-ranks of the step time)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
     return rank, world, local
 
 
@@ -118,13 +122,21 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
+    """The largest x over all ranks (the job's time is its slowest rank's)."""
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_throughput(units_per_rank, seconds_max, world, scale=1e-9):
+    """Whole-job throughput: the units all ranks processed over the slowest
+    rank's time (weak scaling: every rank processes units_per_rank)."""
+    return units_per_rank * world / seconds_max * scale
 
 
 def cpu_sort_baseline(sample=1 << 24, trials=3):
@@ -261,7 +273,7 @@ def main():
     ms_total = max_over_ranks(ms_total, world)
     barrier(world)
     ms_step = ms_total / args.steps
-    value = N_SORT * args.steps * world / (ms_total / 1e3) / 1e9
+    value = job_throughput(N_SORT * args.steps, ms_total / 1e3, world)
     # correctness of the last timed step (cheap property check)
     k_last = bufs[-1][0].to(torch.int64) & 0xFFFFFFFF
     sorted_ok = bool((k_last[1:] >= k_last[:-1]).all())
@@ -369,7 +381,7 @@ def run_e2e(torch, bc, rank, world):
         bc.sort_by_key_host(hk, hv, dtype="uint")
         tot += time.perf_counter() - t0
     tot = max_over_ranks(tot, world)
-    return {"value": N_SORT * e2e_steps * world / tot / 1e9, "unit": "Gkeys/s",
+    return {"value": job_throughput(N_SORT * e2e_steps, tot, world), "unit": "Gkeys/s",
             "h2d_bytes_per_step": 8 * N_SORT, "d2h_bytes_per_step": 8 * N_SORT,
             "ms_per_step": tot / e2e_steps * 1e3, "steps": e2e_steps,
             "path": "bcx_sort_pairs_host (pinned host buffers)"}
