@@ -557,8 +557,9 @@ def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205):
         tune_s = time.perf_counter() - t0
         tuned = [ln for ln in rep.value.decode().splitlines() if "->" in ln]
         tb = C.c_size_t(0)
-        L.bcx_segmented_sort_pairs(st, DTYPES["uint"], 4, None, None, n, offs.data_ptr(), nseg, 0, None,
-                                   C.byref(tb))
+        rc = L.bcx_segmented_sort_pairs(st, DTYPES["uint"], 4, keys.data_ptr(), vals.data_ptr(), n, offs.data_ptr(),
+                                        nseg, 0, None, C.byref(tb))
+        assert rc == 0, L.bcx_last_error_string()
         temp = torch.empty(tb.value, dtype=torch.uint8, device=dev)
 
         def seg_sort():
@@ -619,8 +620,9 @@ def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205):
         assert rc == 0, L.bcx_last_error_string()
         tuned = [ln for ln in rep.value.decode().splitlines() if "->" in ln]
         zero = (C.c_ubyte * 8)()
-        L.bcx_segmented_scan(st, DTYPES["int"], 0, 1, zero, x.data_ptr(), out.data_ptr(), n, offs.data_ptr(), nseg,
-                             0, None, C.byref(tb))
+        rc = L.bcx_segmented_scan(st, DTYPES["int"], 0, 1, zero, x.data_ptr(), out.data_ptr(), n, offs.data_ptr(),
+                                  nseg, 0, None, C.byref(tb))
+        assert rc == 0, L.bcx_last_error_string()
         temp = torch.empty(max(tb.value, 1), dtype=torch.uint8, device=dev)
 
         def seg_scan():
@@ -661,8 +663,9 @@ def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205):
         ko = torch.empty(nseg, dtype=torch.int32, device=dev)
         vo = torch.empty(nseg, dtype=torch.float32, device=dev)
         runs = torch.zeros(1, dtype=torch.int64, device=dev)
-        L.bcx_reduce_by_key(st, DTYPES["int"], DTYPES["float"], 0, seg_id.data_ptr(), v.data_ptr(), n,
-                            ko.data_ptr(), vo.data_ptr(), runs.data_ptr(), 1, None, C.byref(tb))
+        rc = L.bcx_reduce_by_key(st, DTYPES["int"], DTYPES["float"], 0, seg_id.data_ptr(), v.data_ptr(), n,
+                                 ko.data_ptr(), vo.data_ptr(), runs.data_ptr(), 1, None, C.byref(tb))
+        assert rc == 0, L.bcx_last_error_string()
         temp = torch.empty(max(tb.value, 1), dtype=torch.uint8, device=dev)
 
         def rbk():
@@ -689,8 +692,9 @@ def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205):
         tuned = [ln for ln in rep.value.decode().splitlines() if "->" in ln]
         so = torch.empty(nseg, dtype=torch.float32, device=dev)
         zf = (C.c_ubyte * 8)()
-        L.bcx_segmented_reduce(st, DTYPES["float"], 0, v.data_ptr(), offs.data_ptr(), nseg, zf, None, 1, None,
-                               C.byref(tb))
+        rc = L.bcx_segmented_reduce(st, DTYPES["float"], 0, v.data_ptr(), offs.data_ptr(), nseg, zf, so.data_ptr(),
+                                    1, None, C.byref(tb))
+        assert rc == 0, L.bcx_last_error_string()
         temp2 = torch.empty(max(tb.value, 1), dtype=torch.uint8, device=dev)
 
         def segred():

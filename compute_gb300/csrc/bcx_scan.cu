@@ -34,8 +34,9 @@
 namespace bcx {
 namespace {
 
-constexpr int kScanThreads = 128;
-constexpr int kScanWarps = kScanThreads / kWarp;
+// Block size of the allocating scan (the no-alloc entry point keeps its own
+// fixed shape).
+constexpr int kScanThreads = 256;
 
 enum : uint32_t { kFlagInvalid = 0, kFlagAggregate = 1, kFlagPrefix = 2 };
 
@@ -277,16 +278,17 @@ __device__ __forceinline__ void load_chunk(const T *__restrict__ in, size_t vi, 
   }
 }
 
-// One block = one tile of kScanThreads * V vectors.
-template <class T, class P, int V, bool SINGLE, class Status>
-__global__ void __launch_bounds__(kScanThreads)
+// One block = one tile of THREADS * V vectors.
+template <class T, class P, int THREADS, int V, bool SINGLE, class Status>
+__global__ void __launch_bounds__(THREADS)
 scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t head_pad,
                  int vec_ok, int exclusive, typename P::Carry init_carry, Status st,
                  uint32_t *tile_counter, uint32_t *err) {
   typedef typename P::Acc Acc;
   typedef typename P::Carry Carry;
   constexpr int N = 16 / sizeof(T);
-  __shared__ Acc warp_tot[kScanWarps];
+  constexpr int WARPS = THREADS / kWarp;
+  __shared__ Acc warp_tot[WARPS];
   __shared__ Carry tile_prefix;
   __shared__ uint32_t tile_slot;
 
@@ -299,7 +301,7 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
     tile = tile_slot;
   }
   const size_t nv = n + head_pad;
-  const size_t tile_vec0 = tile * size_t(kScanThreads) * V;
+  const size_t tile_vec0 = tile * size_t(THREADS) * V;
   const size_t warp_vec0 = tile_vec0 + size_t(warp) * kWarp * V;
 
   T x[V][N];
@@ -332,7 +334,7 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   Acc warp_excl = P::ident();
   Acc tile_agg = P::ident();
 #pragma unroll
-  for (int w = 0; w < kScanWarps; ++w) {
+  for (int w = 0; w < WARPS; ++w) {
     if (w == int(warp)) warp_excl = tile_agg;
     tile_agg = P::comb(tile_agg, warp_tot[w]);
   }
@@ -382,7 +384,12 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   }
 }
 
-template <class T> struct scan_vectors_per_thread { static constexpr int value = 8; };
+// 16-byte vectors per thread: 64 elements per thread when the accumulator is
+// at most 4 bytes (64 KB tiles of 4-byte elements), 32 compensated FP32
+// pairs, 8 elements of 8-byte types; larger shapes spill registers.
+template <class T, class P> struct scan_vectors_per_thread {
+  static constexpr int value = sizeof(typename P::Acc) <= 4 ? int(64 / (16 / sizeof(T))) : (sizeof(T) == 4 ? 8 : 4);
+};
 
 template <class T, class P>
 bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const void *in, void *out,
@@ -390,7 +397,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   typedef typename P::Carry Carry;
   typedef TileStatus<Carry> Status;
   constexpr int N = 16 / sizeof(T);
-  constexpr int V = scan_vectors_per_thread<T>::value;
+  constexpr int V = scan_vectors_per_thread<T, P>::value;
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;
@@ -413,7 +420,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   if (single) {
     Status st{};
     KernelScope ks("scan_single", s);
-    scan_tile_kernel<T, P, V, true, Status><<<1, kScanThreads, 0, s>>>(
+    scan_tile_kernel<T, P, kScanThreads, V, true, Status><<<1, kScanThreads, 0, s>>>(
         pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, nullptr, ds->err_word);
     return launch_status("scan_single");
   }
@@ -424,7 +431,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
   BCX_CHECK(tiles < (size_t(1) << 31), BCX_INVALID_VALUE, "scan: input too large");
   KernelScope ks("scan_lookback", s);
-  scan_tile_kernel<T, P, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
+  scan_tile_kernel<T, P, kScanThreads, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
       pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);
   return launch_status("scan_lookback");
 }
@@ -516,6 +523,7 @@ namespace bcx {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
+constexpr int kNoAllocThreads = 128;
 constexpr int kNoAllocVectorsPerThread = 4;
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[kNoAllocScratchBytes];
 
@@ -561,7 +569,7 @@ bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, c
   const bool elem_aligned = (ain % sizeof(T) == 0) && (aout % sizeof(T) == 0);
   const bool vec_ok = elem_aligned && ((ain & 15u) == (aout & 15u));
   const size_t head_pad = vec_ok ? (ain & 15u) / sizeof(T) : 0;
-  const size_t tile_elems = size_t(kScanThreads) * V * N;
+  const size_t tile_elems = size_t(kNoAllocThreads) * V * N;
   const size_t tiles = div_up(n + head_pad, tile_elems);
   const Carry init_carry = P::host_carry(init);
   const T *pin = static_cast<const T *>(in);
@@ -569,7 +577,7 @@ bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, c
   if (tiles <= 1) {
     Status st{};
     KernelScope ks("scan_single", s);
-    scan_tile_kernel<T, P, V, true, Status><<<1, kScanThreads, 0, s>>>(
+    scan_tile_kernel<T, P, kNoAllocThreads, V, true, Status><<<1, kNoAllocThreads, 0, s>>>(
         pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, nullptr, ds->err_word);
     return launch_status("scan_single");
   }
@@ -594,7 +602,7 @@ bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, c
   // The array keeps the previous call's tickets and flags: clear them.
   BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
   KernelScope ks("scan_lookback", s);
-  scan_tile_kernel<T, P, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
+  scan_tile_kernel<T, P, kNoAllocThreads, V, false, Status><<<unsigned(tiles), kNoAllocThreads, 0, s>>>(
       pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);
   return launch_status("scan_lookback");
 }

@@ -309,8 +309,8 @@ bcx_status bcx_tune_segmented_sort_pairs(bcx_stream stream, bcx_dtype key_type, 
   Scratch sc;
   void *k2 = nullptr, *v2 = nullptr, *tmp = nullptr;
   size_t tb = 0;
-  bcx_status rc = bcx_segmented_sort_pairs(stream, key_type, value_bytes, nullptr, nullptr, n, offsets, nseg, 0,
-                                           nullptr, &tb);
+  bcx_status rc = bcx_segmented_sort_pairs(stream, key_type, value_bytes, const_cast<void *>(keys),
+                                           const_cast<void *>(values), n, offsets, nseg, 0, nullptr, &tb);
   if (rc) return rc;
   if ((rc = sc.alloc(&k2, n * kb)) || (rc = sc.alloc(&v2, n * value_bytes)) || (rc = sc.alloc(&tmp, tb))) return rc;
   const std::function<bcx_status()> reset = [&]() -> bcx_status {
@@ -375,9 +375,11 @@ bcx_status bcx_tune_segmented_reduce(bcx_stream stream, bcx_dtype type, const vo
   Scratch sc;
   void *out = nullptr, *tmp = nullptr;
   size_t tb = 0;
-  bcx_status rc = bcx_segmented_reduce(stream, type, BCX_PLUS, in, offsets, nseg, zero, nullptr, comp, nullptr, &tb);
+  bcx_status rc = sc.alloc(&out, nseg * es);
   if (rc) return rc;
-  if ((rc = sc.alloc(&out, nseg * es)) || (rc = sc.alloc(&tmp, tb))) return rc;
+  rc = bcx_segmented_reduce(stream, type, BCX_PLUS, in, offsets, nseg, zero, out, comp, nullptr, &tb);
+  if (rc) return rc;
+  if ((rc = sc.alloc(&tmp, tb))) return rc;
   const std::function<bcx_status()> reset = [] { return BCX_SUCCESS; };
   auto run = [&]() -> bcx_status {
     size_t t = tb;
