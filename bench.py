@@ -42,9 +42,11 @@ WORKLOAD = ("sort_by_key uint32 keys (uniform 32-bit) with uint32 values (iota),
 # (8 B read + 8 B write) = 68 B/pair; one onesweep pass = 16 B/pair.
 SORT_BYTES_PER_PAIR = 68
 ONESWEEP_BYTES_PER_PAIR = 16
-# DRAM traffic of one onesweep launch per pair, from the ncu capture summarised
-# in profiles/radix_onesweep_u32_pairs.md (None until captured).
-ONESWEEP_DRAM_BYTES_PER_PAIR = None
+# DRAM traffic of one onesweep launch per pair: dram__bytes_read.sum +
+# dram__bytes_write.sum of one captured launch at 2^25 pairs (502.4 MB), per
+# pair, scaled to the 2^28-pair launch by the pairs it moves
+# (profiles/radix_onesweep_u32_pairs.md).
+ONESWEEP_DRAM_BYTES_PER_PAIR = 502.352384e6 / (1 << 25)
 
 
 def peaks():
@@ -341,6 +343,24 @@ def main():
 
 def run_primitives(torch, bc, dev, g, psteps, hbm):
     prims = {}
+    # README example: compute::sort of 2^20 float32 integers in [0, 2^31-1]
+    # (launch-bound at this size: reported, not a roofline target)
+    n_small = 1 << 20
+    base = torch.randint(0, 2**31 - 1, (n_small,), dtype=torch.int64, device=dev, generator=g).to(torch.float32)
+    bufs = [base.clone() for _ in range(psteps + 3)]
+    for i in range(3):
+        bc.sort(bufs[i])
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for i in range(3, psteps + 3):
+        bc.sort(bufs[i])
+    b.record()
+    b.synchronize()
+    ms = a.elapsed_time(b) / psteps
+    prims["sort_f32_readme_2p20"] = {"us": ms * 1e3, "Gkeys/s": n_small / ms / 1e6,
+                                     "sorted": bool((bufs[-1][1:] >= bufs[-1][:-1]).all())}
+    del bufs, base
     a = torch.randint(0, 100, (N_SCAN,), dtype=torch.int32, device=dev, generator=g)
     out = torch.empty_like(a)
     red = torch.zeros(1, dtype=torch.int32, device=dev)

@@ -30,8 +30,6 @@ namespace {
 
 constexpr int kRbkThreads = 256;
 constexpr int kRbkWarps = kRbkThreads / kWarp;
-constexpr int kRbkItems = 8;
-constexpr int kRbkTile = kRbkThreads * kRbkItems;
 constexpr uint32_t kHeadBit = 0x80000000u;
 constexpr uint32_t kCountMask = 0x7fffffffu;
 enum : uint32_t { kRbInvalid = 0, kRbAggregate = 1, kRbPrefix = 2 };
@@ -111,13 +109,46 @@ struct RbStatus {
 template <class K>
 __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 
+// Tile shape: every lane owns N consecutive elements per chunk (one vector
+// load of keys and one of values when aligned), CH chunks per thread, 16
+// elements per thread in all.
+template <class K, class V>
+struct RbkShape {
+  static constexpr int W = sizeof(K) > sizeof(V) ? int(sizeof(K)) : int(sizeof(V));
+  static constexpr int N = 16 / W;
+  static constexpr int CH = 16 / N;
+  static constexpr int TILE = kRbkThreads * N * CH;
+};
+
+template <class T, int N>
+struct alignas(sizeof(T) * N) VecN {
+  T v[N];
+};
+
+// Elements e0 .. e0+N-1 (e0 a multiple of N): one vector load when the array
+// is aligned to the vector and the run is in range, else element loads.
+template <class T, int N>
+__device__ __forceinline__ void load_run(const T *__restrict__ p, size_t e0, size_t n, bool vec, T (&x)[N]) {
+  if (vec && e0 + N <= n) {
+    const VecN<T, N> w = *reinterpret_cast<const VecN<T, N> *>(p + e0);
+#pragma unroll
+    for (int m = 0; m < N; ++m) x[m] = w.v[m];
+  } else {
+#pragma unroll
+    for (int m = 0; m < N; ++m) x[m] = (e0 + m < n) ? p[e0 + m] : T(0);
+  }
+}
+
 template <class K, class V, class P>
 __global__ void __launch_bounds__(kRbkThreads)
 reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uint32_t n,
                      K *__restrict__ keys_out, V *__restrict__ vals_out,
                      unsigned long long *__restrict__ num_runs, RbStatus<P> st,
-                     uint32_t *__restrict__ tile_counter, int single, uint32_t *err) {
+                     uint32_t *__restrict__ tile_counter, int single, int vec_k, int vec_v, uint32_t *err) {
   typedef Seg<P> S;
+  typedef RbkShape<K, V> Sh;
+  constexpr int N = Sh::N;
+  constexpr int CH = Sh::CH;
   __shared__ S s_warp[kRbkWarps];
   __shared__ S s_prefix;
   __shared__ uint32_t s_tile;
@@ -128,44 +159,51 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
     __syncthreads();
     tile = s_tile;
   }
-  const uint32_t warp_base = tile * kRbkTile + warp * (kWarp * kRbkItems);
+  // Warp w covers CH chunks of 32*N consecutive elements; in chunk j lane l
+  // owns elements chunk_base + l*N .. + N-1, so (j, l, m) is input order.
+  const size_t warp_base = size_t(tile) * Sh::TILE + size_t(warp) * (CH * kWarp * N);
 
-  K k[kRbkItems];
-  V v[kRbkItems];
+  K k[CH][N];
+  V v[CH][N];
 #pragma unroll
-  for (int i = 0; i < kRbkItems; ++i) {
-    const uint32_t idx = warp_base + i * kWarp + lane;
-    if (idx < n) {
-      k[i] = keys[idx];
-      v[i] = vals[idx];
-    } else {
-      k[i] = K(0);
-      v[i] = V(0);
-    }
+  for (int j = 0; j < CH; ++j) {
+    const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
+    load_run<K, N>(keys, e0, n, vec_k != 0, k[j]);
+    load_run<V, N>(vals, e0, n, vec_v != 0, v[j]);
   }
-  // Head flags: previous element is lane-1 of the same item, lane 31 of the
-  // previous item, or (item 0, lane 0) the element before this warp's run.
-  uint32_t head_mask = 0;  // bit i = element of item i is a run head
+  // Head flags: bit j*N+m = element (j, m) starts a run.
+  uint32_t heads = 0;
   const K before = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);
 #pragma unroll
-  for (int i = 0; i < kRbkItems; ++i) {
-    const uint32_t idx = warp_base + i * kWarp + lane;
-    K prev = __shfl_up_sync(0xffffffffu, k[i], 1);
-    const K last_prev_item = __shfl_sync(0xffffffffu, k[i > 0 ? i - 1 : 0], kWarp - 1);
-    if (lane == 0) prev = (i > 0) ? last_prev_item : before;
-    const bool h = (idx < n) && (idx == 0 || !keys_equal(prev, k[i]));
-    head_mask |= uint32_t(h) << i;
+  for (int j = 0; j < CH; ++j) {
+    const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
+    K prev = __shfl_up_sync(0xffffffffu, k[j][N - 1], 1);
+    const K last_prev_chunk = __shfl_sync(0xffffffffu, k[j > 0 ? j - 1 : 0][N - 1], kWarp - 1);
+    if (lane == 0) prev = j > 0 ? last_prev_chunk : before;
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const size_t idx = e0 + m;
+      const K p = m > 0 ? k[j][m - 1] : prev;
+      const bool h = idx < n && (idx == 0 || !keys_equal(p, k[j][m]));
+      heads |= uint32_t(h) << (j * N + m);
+    }
   }
-  // Per item: warp inclusive segmented scan (lane_incl), carried across items.
-  S lane_incl[kRbkItems];
+  // Per chunk: serial fold of the lane's N elements, warp scan of the lane
+  // folds, carried across chunks.
+  S lane_excl[CH], chunk_pre[CH];
   S run = seg_ident<P>();
 #pragma unroll
-  for (int i = 0; i < kRbkItems; ++i) {
-    const uint32_t idx = warp_base + i * kWarp + lane;
-    S x;
-    const bool h = (head_mask >> i) & 1u;
-    x.c = h ? (kHeadBit | 1u) : 0u;
-    x.v = (idx < n) ? P::from(v[i]) : P::ident();
+  for (int j = 0; j < CH; ++j) {
+    const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
+    S a = seg_ident<P>();
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      S e;
+      e.c = ((heads >> (j * N + m)) & 1u) ? (kHeadBit | 1u) : 0u;
+      e.v = (e0 + m < n) ? P::from(v[j][m]) : P::ident();
+      a = seg_comb<P>(a, e);
+    }
+    S x = a;
 #pragma unroll
     for (int d = 1; d < kWarp; d <<= 1) {
       S o;
@@ -173,7 +211,11 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
       o.v = P::shfl_up(x.v, d);
       if (int(lane) >= d) x = seg_comb<P>(o, x);
     }
-    lane_incl[i] = x;
+    S ex;
+    ex.c = __shfl_up_sync(0xffffffffu, x.c, 1);
+    ex.v = P::shfl_up(x.v, 1);
+    lane_excl[j] = lane == 0 ? seg_ident<P>() : ex;
+    chunk_pre[j] = run;
     S tot;
     tot.c = __shfl_sync(0xffffffffu, x.c, kWarp - 1);
     tot.v = P::shfl(x.v, kWarp - 1);
@@ -211,7 +253,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
               val = seg_ident<P>();
               break;
             }
-            __nanosleep(spins < 64 ? 32 : 256);
+            if (spins > 16) __nanosleep(64);
             f = st.poll(size_t(t), &val);
           }
         }
@@ -239,30 +281,35 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
     if (lane == 0) s_prefix = excl;
   }
   __syncthreads();
-  // Emit: heads write keys, run ends write values.
-  S pre = seg_comb<P>(s_prefix, warp_excl);
+  // Emit: run heads write their key, run ends their reduced value.
+  const S pre = seg_comb<P>(s_prefix, warp_excl);
+  const size_t warp_end = warp_base + size_t(CH) * kWarp * N;  // first element after this warp
+  const bool after_head = warp_end < n && !keys_equal(k[CH - 1][N - 1], lane == kWarp - 1 ? keys[warp_end] : k[CH - 1][N - 1]);
 #pragma unroll
-  for (int i = 0; i < kRbkItems; ++i) {
-    const uint32_t idx = warp_base + i * kWarp + lane;
-    const S incl = seg_comb<P>(pre, lane_incl[i]);
-    const bool h = (head_mask >> i) & 1u;
-    // next element's head flag
-    bool next_head = __shfl_down_sync(0xffffffffu, h ? 1u : 0u, 1) != 0;
-    const uint32_t next_item_h0 = __shfl_sync(0xffffffffu, (head_mask >> (i + 1 < kRbkItems ? i + 1 : i)) & 1u, 0);
-    if (lane == kWarp - 1) {
-      if (i + 1 < kRbkItems) next_head = next_item_h0 != 0;
-      else next_head = (idx + 1 < n) ? !keys_equal(keys[idx + 1], k[i]) : true;
+  for (int j = 0; j < CH; ++j) {
+    const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
+    // head flag of the element after this lane's run in chunk j
+    const uint32_t h_next_lane = __shfl_down_sync(0xffffffffu, heads >> (j * N), 1) & 1u;
+    const uint32_t h_next_chunk = __shfl_sync(0xffffffffu, heads >> (j + 1 < CH ? (j + 1) * N : 0), 0) & 1u;
+    uint32_t next_h = h_next_lane;
+    if (lane == kWarp - 1) next_h = j + 1 < CH ? h_next_chunk : uint32_t(after_head);
+    S acc = seg_comb<P>(seg_comb<P>(pre, chunk_pre[j]), lane_excl[j]);
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const size_t idx = e0 + m;
+      const bool h = (heads >> (j * N + m)) & 1u;
+      S e;
+      e.c = h ? (kHeadBit | 1u) : 0u;
+      e.v = idx < n ? P::from(v[j][m]) : P::ident();
+      acc = seg_comb<P>(acc, e);
+      if (idx < n) {
+        const uint32_t run_idx = (acc.c & kCountMask) - 1u;
+        const bool last = idx + 1 == n || (m + 1 < N ? ((heads >> (j * N + m + 1)) & 1u) != 0 : next_h != 0);
+        if (h && keys_out) keys_out[run_idx] = k[j][m];
+        if (last) vals_out[run_idx] = P::out(acc.v);
+        if (idx + 1 == n) *num_runs = (unsigned long long)(acc.c & kCountMask);
+      }
     }
-    if (idx < n) {
-      const uint32_t run_idx = (incl.c & kCountMask) - 1u;
-      if (h && keys_out) keys_out[run_idx] = k[i];
-      if (idx + 1 == n || next_head) vals_out[run_idx] = P::out(incl.v);
-      if (idx + 1 == n) *num_runs = (unsigned long long)(incl.c & kCountMask);
-    }
-    S tot;
-    tot.c = __shfl_sync(0xffffffffu, lane_incl[i].c, kWarp - 1);
-    tot.v = P::shfl(lane_incl[i].v, kWarp - 1);
-    pre = seg_comb<P>(pre, tot);
   }
 }
 
@@ -270,10 +317,11 @@ template <class K, class V, class P>
 bcx_status run_rbk(cudaStream_t s, const void *keys, const void *vals, size_t n, void *keys_out,
                    void *vals_out, uint64_t *num_runs, void *temp, size_t *temp_bytes) {
   typedef Seg<P> S;
+  typedef RbkShape<K, V> Sh;
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;
-  const size_t tiles = div_up(n, kRbkTile);
+  const size_t tiles = div_up(n, size_t(Sh::TILE));
   const bool single = tiles <= 1;
   const size_t need = single ? 0 : 256 + align256(tiles * 4) + 2 * align256(tiles * sizeof(S));
   TempStorage ts;
@@ -290,11 +338,13 @@ bcx_status run_rbk(cudaStream_t s, const void *keys, const void *vals, size_t n,
     st.inc = reinterpret_cast<S *>(base + 256 + align256(tiles * 4) + align256(tiles * sizeof(S)));
     BCX_CUDA(cudaMemsetAsync(base, 0, 256 + align256(tiles * 4), s));
   }
+  const int vec_k = reinterpret_cast<uintptr_t>(keys) % (sizeof(K) * Sh::N) == 0;
+  const int vec_v = reinterpret_cast<uintptr_t>(vals) % (sizeof(V) * Sh::N) == 0;
   KernelScope ks("reduce_by_key", s);
   reduce_by_key_kernel<K, V, P><<<unsigned(tiles), kRbkThreads, 0, s>>>(
       static_cast<const K *>(keys), static_cast<const V *>(vals), uint32_t(n), static_cast<K *>(keys_out),
       static_cast<V *>(vals_out), reinterpret_cast<unsigned long long *>(num_runs), st, counter,
-      single ? 1 : 0, ds->err_word);
+      single ? 1 : 0, vec_k, vec_v, ds->err_word);
   return launch_status("reduce_by_key");
 }
 

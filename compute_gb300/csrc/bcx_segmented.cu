@@ -128,14 +128,26 @@ __device__ __forceinline__ size_t lower_bound_u64(const unsigned long long *offs
   return lo;
 }
 
+template <class T, int N>
+struct alignas(sizeof(T) * N) SegVec {
+  T v[N];
+};
+
+// ITEMS elements per thread in ITEMS/N chunks; in chunk j lane l owns the N
+// consecutive elements chunk_base + l*N .. + N-1 (one vector load and store
+// when the arrays are aligned), so (j, l, m) is input order within a warp.
 template <class T, class P, int ITEMS>
 __global__ void __launch_bounds__(kSegThreads)
 segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
                       const unsigned long long *__restrict__ offsets, size_t nseg, int exclusive,
-                      typename P::Acc init, SgStatus<P> st, uint32_t *__restrict__ tile_counter,
-                      uint32_t *err) {
+                      typename P::Acc init, SgStatus<P> st, uint32_t *__restrict__ tile_counter, int vec_in,
+                      int vec_out, uint32_t *err) {
   typedef Sg<P> S;
+  typedef typename P::Acc Acc;
+  constexpr int N = 16 / int(sizeof(T)) < ITEMS ? 16 / int(sizeof(T)) : ITEMS;
+  constexpr int CH = ITEMS / N;
   constexpr int TILE = kSegThreads * ITEMS;
+  static_assert(32 % N == 0, "a lane's run sits inside one bitmap word");
   __shared__ uint32_t s_heads[TILE / 32];
   __shared__ S s_warp[kSegWarps];
   __shared__ S s_prefix;
@@ -158,30 +170,47 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
       atomicOr(&s_heads[local >> 5], 1u << (local & 31u));
     }
   }
-  __syncthreads();
   const uint32_t warp_first = warp * (kWarp * ITEMS);
-  T x[ITEMS];
+  T x[CH][N];
 #pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const size_t idx = tile_base + warp_first + i * kWarp + lane;
-    x[i] = idx < n ? in[idx] : T(0);
+  for (int j = 0; j < CH; ++j) {
+    const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
+    if (vec_in && e0 + N <= n) {
+      const SegVec<T, N> w = *reinterpret_cast<const SegVec<T, N> *>(in + e0);
+#pragma unroll
+      for (int m = 0; m < N; ++m) x[j][m] = w.v[m];
+    } else {
+#pragma unroll
+      for (int m = 0; m < N; ++m) x[j][m] = (e0 + m < n) ? in[e0 + m] : T(0);
+    }
   }
-  S lane_incl[ITEMS];
+  __syncthreads();
+  uint32_t hb[CH];  // head bits of the lane's run in chunk j (bit m)
+#pragma unroll
+  for (int j = 0; j < CH; ++j) {
+    const uint32_t local = warp_first + j * (kWarp * N) + lane * N;
+    hb[j] = (s_heads[local >> 5] >> (local & 31u)) & ((1u << N) - 1u);
+  }
+  S lane_excl[CH], chunk_pre[CH];
   S run = sg_ident<P>();
 #pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const uint32_t local = warp_first + i * kWarp + lane;
-    const size_t idx = tile_base + local;
-    S e;
-    e.h = (s_heads[local >> 5] >> (local & 31u)) & 1u;
-    e.v = idx < n ? P::from(x[i]) : P::ident();
+  for (int j = 0; j < CH; ++j) {
+    const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
+    S a = sg_ident<P>();
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const S e{(hb[j] >> m) & 1u, (e0 + m < n) ? P::from(x[j][m]) : P::ident()};
+      a = sg_comb<P>(a, e);
+    }
 #pragma unroll
     for (int d = 1; d < kWarp; d <<= 1) {
-      const S o = sg_shfl_up<P>(e, d);
-      if (int(lane) >= d) e = sg_comb<P>(o, e);
+      const S o = sg_shfl_up<P>(a, d);
+      if (int(lane) >= d) a = sg_comb<P>(o, a);
     }
-    lane_incl[i] = e;
-    run = sg_comb<P>(run, sg_shfl<P>(e, kWarp - 1));
+    const S ex = sg_shfl_up<P>(a, 1);
+    lane_excl[j] = lane == 0 ? sg_ident<P>() : ex;
+    chunk_pre[j] = run;
+    run = sg_comb<P>(run, sg_shfl<P>(a, kWarp - 1));
   }
   if (lane == 0) s_warp[warp] = run;
   __syncthreads();
@@ -235,32 +264,32 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
     if (lane == 0) s_prefix = excl;
   }
   __syncthreads();
-  // Inclusive value of every element; the exclusive output of element i is
-  // init op (inclusive of i-1 if i continues a segment).
-  S pre = sg_comb<P>(s_prefix, warp_excl);
-  typename P::Acc prev_last = P::ident();  // inclusive value of the element before item i, lane 0
-  uint32_t prev_last_valid = 0;
-  {
-    // the element before this warp's first item: the tile/warp prefix itself
-    prev_last = pre.v;
-    prev_last_valid = 1;
-  }
+  // Inclusive output: the running value after each element.  Exclusive
+  // output: init for a segment's first element, else init op the running
+  // value before it.
+  const S pre = sg_comb<P>(s_prefix, warp_excl);
 #pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const uint32_t local = warp_first + i * kWarp + lane;
-    const size_t idx = tile_base + local;
-    const S incl = sg_comb<P>(pre, lane_incl[i]);
-    if (exclusive) {
-      typename P::Acc before = P::shfl_up(incl.v, 1);
-      if (lane == 0) before = prev_last;
-      const uint32_t h = (s_heads[local >> 5] >> (local & 31u)) & 1u;
-      const typename P::Acc e = (h || (lane == 0 && !prev_last_valid)) ? init : P::comb(init, before);
-      if (idx < n) out[idx] = P::out(e);
-    } else {
-      if (idx < n) out[idx] = P::out(incl.v);
+  for (int j = 0; j < CH; ++j) {
+    const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
+    S acc = sg_comb<P>(sg_comb<P>(pre, chunk_pre[j]), lane_excl[j]);
+    T y[N];
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const uint32_t h = (hb[j] >> m) & 1u;
+      const Acc ex = h ? init : P::comb(init, acc.v);
+      acc = sg_comb<P>(acc, S{h, (e0 + m < n) ? P::from(x[j][m]) : P::ident()});
+      y[m] = P::out(exclusive ? ex : acc.v);
     }
-    prev_last = P::shfl(incl.v, kWarp - 1);
-    pre = sg_comb<P>(pre, sg_shfl<P>(lane_incl[i], kWarp - 1));
+    if (vec_out && e0 + N <= n) {
+      SegVec<T, N> w;
+#pragma unroll
+      for (int m = 0; m < N; ++m) w.v[m] = y[m];
+      *reinterpret_cast<SegVec<T, N> *>(out + e0) = w;
+    } else {
+#pragma unroll
+      for (int m = 0; m < N; ++m)
+        if (e0 + m < n) out[e0 + m] = y[m];
+    }
   }
 }
 
@@ -315,10 +344,13 @@ bcx_status launch_segmented_scan(cudaStream_t s, int exclusive, const T &init_v,
                                  size_t n, const unsigned long long *offsets, size_t nseg, char *base,
                                  const SgStatus<P> &st, DeviceState *ds) {
   const size_t tiles = div_up(n, size_t(kSegThreads) * ITEMS);
+  constexpr int N = 16 / int(sizeof(T)) < ITEMS ? 16 / int(sizeof(T)) : ITEMS;
+  const int vec_in = reinterpret_cast<uintptr_t>(in) % (sizeof(T) * N) == 0;
+  const int vec_out = reinterpret_cast<uintptr_t>(out) % (sizeof(T) * N) == 0;
   KernelScope ks("segmented_scan", s);
   segmented_scan_kernel<T, P, ITEMS><<<unsigned(tiles), kSegThreads, 0, s>>>(
       static_cast<const T *>(in), static_cast<T *>(out), n, offsets, nseg, exclusive, P::from_host(init_v), st,
-      reinterpret_cast<uint32_t *>(base), ds->err_word);
+      reinterpret_cast<uint32_t *>(base), vec_in, vec_out, ds->err_word);
   return launch_status("segmented_scan");
 }
 
