@@ -772,7 +772,8 @@ def make_serving_requests(count, seed, lo=10, hi=26):
     return kinds, dtypes, ns, offs
 
 
-def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo=10, hi=26, slots=8):
+def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo=10, hi=26, slots=8,
+                small_limit=None, batch_elems=0, batch_count=0, baselines=True):
     """Open-loop Poisson arrivals of device-resident requests through the
     continuous-batching server, against the same requests issued as serial
     plain C-ABI calls (each waited for before the next, as a caller that needs
@@ -849,25 +850,31 @@ def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo
     for r in reqs[:20]:
         assert plain(r) == 0
     L.bcx_stream_synchronize(stream)
+    if not baselines:  # server only (configuration sweeps)
+        reqs_for_baseline = []
+    else:
+        reqs_for_baseline = reqs
     per_call = []
     t0 = time.perf_counter()
-    for r in reqs:
+    for r in reqs_for_baseline:
         a = time.perf_counter()
         rc = plain(r)
         L.bcx_stream_synchronize(stream)
         per_call.append(time.perf_counter() - a)
         assert rc == 0
-    serial_s = time.perf_counter() - t0
+    serial_s = max(time.perf_counter() - t0, 1e-9)
     t0 = time.perf_counter()
-    for r in reqs:
+    for r in reqs_for_baseline:
         plain(r)
     L.bcx_stream_synchronize(stream)
-    queued_s = time.perf_counter() - t0
-    per_call_ms = np.array(per_call) * 1e3
+    queued_s = max(time.perf_counter() - t0, 1e-9)
+    per_call_ms = np.array(per_call if per_call else [0.0]) * 1e3
     out = {"requests_per_rate": count, "elements": int(elems), "bytes_per_pass": int(bytes_moved),
            "mix": "50% sort_by_key (values uint32) / 30% exclusive_scan / 20% reduce; "
                   f"n log-uniform [2^{lo}, 2^{hi}]; dtype uniform int32/uint32/float32/uint64; "
                   "device-resident inputs, per-request outputs",
+           "server": {"slots": slots, "small_limit": small_limit if small_limit is not None else 1 << 18,
+                      "batch_elems": batch_elems or 1 << 24, "batch_count": batch_count or 4096},
            "serial_plain": {"req_per_s": count / serial_s, "GB_per_s": bytes_moved / serial_s / 1e9,
                             "p50_ms": float(np.percentile(per_call_ms, 50)),
                             "p99_ms": float(np.percentile(per_call_ms, 99)),
@@ -878,7 +885,7 @@ def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo
 
     # -- the server, open-loop Poisson arrivals
     rng = np.random.default_rng(seed + 1)
-    with Server(slots=slots) as srv:
+    with Server(slots=slots, small_limit=small_limit, batch_elems=batch_elems, batch_count=batch_count) as srv:
         for r in reqs[:20]:
             srv.wait(srv.submit_request(r))
         for rate in rates:
