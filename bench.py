@@ -225,6 +225,7 @@ def main():
                     help="'sort' skips the other sections; 'prims', 'precision', 'serve', 'segmented' run a "
                          "2^20 sort and that section only (profiling runs)")
     ap.add_argument("--serve-count", type=int, default=1000, help="requests per arrival rate")
+    ap.add_argument("--seg-count", type=int, default=10_000, help="segments of the segmented workloads")
     ap.add_argument("--n-sort", type=int, default=DEFAULT_N_SORT, help="pairs per sort (default 2^28)")
     ap.add_argument("--n-scan", type=int, default=DEFAULT_N_SCAN, help="scan/reduce elements (default 2^30)")
     args = ap.parse_args()
@@ -309,7 +310,7 @@ def main():
         precision = run_precision(torch, bc, dev, hbm)
     segmented = None
     if args.only in ("all", "segmented"):
-        segmented = run_segmented(torch, bc, dev, hbm)
+        segmented = run_segmented(torch, bc, dev, hbm, nseg=args.seg_count)
     serving = None
     if args.only in ("all", "serve") and world == 1:
         serving = run_serving(torch, bc, dev, count=args.serve_count)
@@ -541,7 +542,7 @@ def _graph_of(torch, fn):
     return g
 
 
-def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205):
+def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205, nseg=10_000):
     """Segmented sort_by_key (uint32/uint32), segmented exclusive_scan (int32)
     and reduce_by_key (float32 N(0,1), keys = segment ids) over 10,000
     log-uniform segments: one launch sequence each, tuned by the autotuner and
@@ -554,8 +555,9 @@ def run_segmented(torch, bc, dev, hbm, steps=3, seed=20261205):
     from compute_gb300._lib import DTYPES, lib
     L = lib()
     results = {}
-    for label, cap in (("10000_segments", None), ("2^28_total", 1 << 28)):
-        offsets = segment_offsets(total_cap=cap, seed=seed)
+    configs = ((f"{nseg}_segments", None), ("2^28_total", 1 << 28)) if nseg == 10_000 else ((f"{nseg}_segments", None),)
+    for label, cap in configs:
+        offsets = segment_offsets(nseg=nseg, total_cap=cap, seed=seed)
         nseg = offsets.size - 1
         n = int(offsets[-1])
         sizes = np.diff(offsets).astype(np.int64)

@@ -39,6 +39,7 @@ struct DeviceState {
   int device = -1;
   int sm_count = 0;
   uint32_t *err_word = nullptr;  // device memory, 4 bytes
+  cudaStream_t aux_stream = nullptr;  // second stream for copies split in two
 };
 // State of the current device (created on first use).
 bcx_status current_device_state(DeviceState **out);

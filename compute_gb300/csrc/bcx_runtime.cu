@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -58,6 +59,20 @@ bcx_status current_device_state(DeviceState **out) {
   BCX_CUDA(cudaDeviceGetAttribute(&st->sm_count, cudaDevAttrMultiProcessorCount, dev));
   BCX_CUDA(cudaMalloc(&st->err_word, sizeof(uint32_t)));
   BCX_CUDA(cudaMemset(st->err_word, 0, sizeof(uint32_t)));
+  // Temporaries come from the device's default stream-ordered pool.  Its
+  // default release threshold (0) hands freed memory back to the driver at
+  // every synchronization, so a sequence of blocking calls would map and unmap
+  // its temporaries each time; keep freed memory cached in the pool instead
+  // (BCX_POOL_RELEASE_THRESHOLD, in bytes, overrides).
+  {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t threshold = UINT64_MAX;
+      if (const char *env = std::getenv("BCX_POOL_RELEASE_THRESHOLD")) threshold = std::strtoull(env, nullptr, 10);
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+  }
+  BCX_CUDA(cudaStreamCreateWithFlags(&st->aux_stream, cudaStreamNonBlocking));
   BCX_CUDA(cudaDeviceSynchronize());
   g_devices[dev] = st;
   *out = st;

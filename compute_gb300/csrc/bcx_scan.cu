@@ -257,23 +257,18 @@ __device__ __forceinline__ typename P::Carry lookback(Status &st, size_t tile,
 
 template <class T>
 __device__ __forceinline__ void load_chunk(const T *__restrict__ in, size_t vi, size_t head_pad,
-                                           size_t nv, bool vec_ok, T (&x)[16 / sizeof(T)],
-                                           bool (&valid)[16 / sizeof(T)]) {
+                                           size_t nv, bool vec_ok, T (&x)[16 / sizeof(T)]) {
   constexpr int N = 16 / sizeof(T);
   const size_t u0 = vi * N;
   if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
     vec16<T> r = ld_stream16(reinterpret_cast<const vec16<T> *>(in - head_pad) + vi);
 #pragma unroll
-    for (int k = 0; k < N; ++k) {
-      x[k] = r.v[k];
-      valid[k] = true;
-    }
+    for (int k = 0; k < N; ++k) x[k] = r.v[k];
   } else {
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       const size_t u = u0 + k;
-      valid[k] = (u >= head_pad && u < nv);
-      x[k] = valid[k] ? in[u - head_pad] : T(0);
+      x[k] = (u >= head_pad && u < nv) ? in[u - head_pad] : T(0);
     }
   }
 }
@@ -305,18 +300,20 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   const size_t warp_vec0 = tile_vec0 + size_t(warp) * kWarp * V;
 
   T x[V][N];
-  bool valid[V][N];
-  Acc lane_excl[V];
-  Acc chunk_pre[V];
+  Acc lane_pre[V];  // prefix of this lane's first element within the warp's part of the tile
   Acc run = P::ident();
+  // element (j, k) lies in [head_pad, nv): the tile's interior is always
+  // in range, only the array's first and last tiles test it
+  const bool interior = (warp_vec0 * N >= head_pad) && (warp_vec0 + size_t(V) * kWarp) * N <= nv;
 #pragma unroll
-  for (int j = 0; j < V; ++j) load_chunk<T>(in, warp_vec0 + size_t(j) * kWarp + lane, head_pad, nv, vec_ok != 0, x[j], valid[j]);
+  for (int j = 0; j < V; ++j) load_chunk<T>(in, warp_vec0 + size_t(j) * kWarp + lane, head_pad, nv, vec_ok != 0, x[j]);
 #pragma unroll
   for (int j = 0; j < V; ++j) {
+    const size_t u0 = (warp_vec0 + size_t(j) * kWarp + lane) * N;
     Acc t = P::ident();
 #pragma unroll
     for (int k = 0; k < N; ++k)
-      if (valid[j][k]) t = P::add(t, x[j][k]);
+      if (interior || (u0 + k >= head_pad && u0 + k < nv)) t = P::add(t, x[j][k]);
     // inclusive warp scan of the per-lane totals of chunk j
     Acc incl = t;
 #pragma unroll
@@ -325,8 +322,7 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
       if (int(lane) >= d) incl = P::comb(o, incl);
     }
     Acc ex = P::shfl_up(incl, 1);
-    lane_excl[j] = (lane == 0) ? P::ident() : ex;
-    chunk_pre[j] = run;
+    lane_pre[j] = (lane == 0) ? run : P::comb(run, ex);
     run = P::comb(run, P::shfl(incl, kWarp - 1));
   }
   if (lane == 0) warp_tot[warp] = run;
@@ -357,20 +353,21 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   T *vout_base = out - head_pad;
 #pragma unroll
   for (int j = 0; j < V; ++j) {
-    Acc r = P::comb(P::comb(base, chunk_pre[j]), lane_excl[j]);
+    const size_t vi = warp_vec0 + size_t(j) * kWarp + lane;
+    const size_t u0 = vi * N;
+    Acc r = P::comb(base, lane_pre[j]);
     T y[N];
 #pragma unroll
     for (int k = 0; k < N; ++k) {
+      const bool ok = interior || (u0 + k >= head_pad && u0 + k < nv);
       if (exclusive) {
         y[k] = P::out(r);
-        if (valid[j][k]) r = P::add(r, x[j][k]);
+        if (ok) r = P::add(r, x[j][k]);
       } else {
-        if (valid[j][k]) r = P::add(r, x[j][k]);
+        if (ok) r = P::add(r, x[j][k]);
         y[k] = P::out(r);
       }
     }
-    const size_t vi = warp_vec0 + size_t(j) * kWarp + lane;
-    const size_t u0 = vi * N;
     if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
       vec16<T> w;
 #pragma unroll
@@ -379,7 +376,7 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
     } else {
 #pragma unroll
       for (int k = 0; k < N; ++k)
-        if (valid[j][k]) vout_base[u0 + k] = y[k];
+        if (u0 + k >= head_pad && u0 + k < nv) vout_base[u0 + k] = y[k];
     }
   }
 }

@@ -116,16 +116,28 @@ struct SgStatus {
   }
 };
 
-// Index of the first offset >= x among offsets[0..count).
-__device__ __forceinline__ size_t lower_bound_u64(const unsigned long long *offsets, size_t count,
-                                                  unsigned long long x) {
-  size_t lo = 0, hi = count;
-  while (lo < hi) {
-    const size_t mid = (lo + hi) / 2;
-    if (offsets[mid] < x) lo = mid + 1;
-    else hi = mid;
+// Index of the first offset >= x among offsets[0..count), found by a whole
+// warp: each step probes 32 evenly spaced entries at once, so 10^4 offsets
+// take three dependent loads instead of fourteen.  Every lane returns the
+// same index.
+__device__ __forceinline__ size_t warp_lower_bound_u64(const unsigned long long *__restrict__ offsets,
+                                                       size_t count, unsigned long long x) {
+  const unsigned lane = lane_id();
+  size_t lo = 0, hi = count;  // the answer lies in [lo, hi]
+  while (hi - lo > size_t(kWarp)) {
+    const size_t step = (hi - lo + kWarp - 1) / kWarp;
+    const size_t p = lo + size_t(lane) * step;
+    const bool ge = p < hi && offsets[p] >= x;
+    const unsigned m = __ballot_sync(0xffffffffu, ge) | __ballot_sync(0xffffffffu, p >= hi);
+    const int f = m ? __ffs(m) - 1 : kWarp;  // first probe at or past the answer
+    if (f == 0) return lo;
+    const size_t below = lo + size_t(f - 1) * step;  // offsets[below] < x
+    hi = (f < kWarp && lo + size_t(f) * step < hi) ? lo + size_t(f) * step : hi;
+    lo = below + 1;
   }
-  return lo;
+  const size_t p = lo + lane;
+  const unsigned m = __ballot_sync(0xffffffffu, p < hi && offsets[p] >= x);
+  return m ? lo + size_t(__ffs(m) - 1) : hi;
 }
 
 template <class T, int N>
@@ -162,7 +174,7 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
   // Mark the segment starts inside this tile (offsets[0..nseg] are starts;
   // offsets[nseg] == n is not).
   if (warp == 0) {
-    const size_t first = lower_bound_u64(offsets, nseg, tile_base);
+    const size_t first = warp_lower_bound_u64(offsets, nseg, tile_base);
     for (size_t k = first + lane; k < nseg; k += kWarp) {
       const unsigned long long o = offsets[k];
       if (o >= tile_end) break;

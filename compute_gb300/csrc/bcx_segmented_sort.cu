@@ -137,13 +137,13 @@ struct LargeTile {
   uint32_t seg, ord, base, count, first_tile;
 };
 
-template <class U>
-__device__ __forceinline__ LargeTile locate_tile(const unsigned long long *__restrict__ offsets,
-                                                 const uint32_t *__restrict__ tile_first,
-                                                 const uint32_t *__restrict__ large_ord, uint32_t nseg, uint32_t t,
-                                                 uint32_t tile) {
+// Large tile t of segment seg: its elements and look-back floor.
+__device__ __forceinline__ LargeTile tile_of_segment(const unsigned long long *__restrict__ offsets,
+                                                     const uint32_t *__restrict__ tile_first,
+                                                     const uint32_t *__restrict__ large_ord, uint32_t seg,
+                                                     uint32_t t, uint32_t tile) {
   LargeTile r;
-  r.seg = segment_of_tile(tile_first, nseg, t);
+  r.seg = seg;
   r.ord = large_ord[r.seg];
   r.first_tile = tile_first[r.seg];
   const unsigned long long b = offsets[r.seg], e = offsets[r.seg + 1];
@@ -159,13 +159,20 @@ __global__ void __launch_bounds__(kHistThreads)
 segsort_hist_kernel(const U *__restrict__ keys, const unsigned long long *__restrict__ offsets, uint32_t nseg,
                     const uint32_t *__restrict__ tile_first, const uint32_t *__restrict__ large_ord,
                     const uint32_t *__restrict__ totals, uint32_t tile, const KeyXform<U> xf,
-                    uint32_t *__restrict__ seg_hist) {
+                    uint32_t *__restrict__ seg_hist, uint32_t *__restrict__ tile_seg) {
   __shared__ uint32_t sh[PASSES][kRadix];
+  __shared__ uint32_t s_seg;
   const uint32_t t = blockIdx.x;
   if (t >= totals[0]) return;
   for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) (&sh[0][0])[i] = 0;
+  // The segment of this tile is searched once here and recorded for the
+  // digit passes.
+  if (threadIdx.x == 0) {
+    s_seg = segment_of_tile(tile_first, nseg, t);
+    tile_seg[t] = s_seg;
+  }
   __syncthreads();
-  const LargeTile lt = locate_tile<U>(offsets, tile_first, large_ord, nseg, t, tile);
+  const LargeTile lt = tile_of_segment(offsets, tile_first, large_ord, s_seg, t, tile);
   for (uint32_t i = threadIdx.x; i < lt.count; i += kHistThreads) {
     const U k = apply_xform<U>(keys[lt.base + i], xf);
 #pragma unroll
@@ -217,14 +224,14 @@ segsort_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
                         const uint32_t *__restrict__ tile_first, const uint32_t *__restrict__ large_ord,
                         const uint32_t *__restrict__ totals, int pass, int passes, const KeyXform<U> xf,
                         const uint32_t *__restrict__ digit_start, uint32_t *__restrict__ status,
-                        uint32_t *__restrict__ tile_counter, uint32_t *err) {
+                        uint32_t *__restrict__ tile_counter, const uint32_t *__restrict__ tile_seg, uint32_t *err) {
   constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
   __shared__ uint32_t s_tile;
   if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
   __syncthreads();
   const uint32_t t = s_tile;
   if (t >= totals[0]) return;
-  const LargeTile lt = locate_tile<U>(offsets, tile_first, large_ord, nseg, t, TILE);
+  const LargeTile lt = tile_of_segment(offsets, tile_first, large_ord, tile_seg[t], t, TILE);
   const bool from_alt = (pass & 1) != 0;
   onesweep_tile<U, VB>(from_alt ? keys_alt : keys_main, from_alt ? keys_main : keys_alt,
                        from_alt ? vals_alt : vals_main, from_alt ? vals_main : vals_alt, lt.base, lt.count, t,
@@ -240,11 +247,11 @@ __global__ void segsort_copyback_kernel(U *__restrict__ keys_main, const U *__re
                                         const unsigned long long *__restrict__ offsets, uint32_t nseg,
                                         const uint32_t *__restrict__ tile_first,
                                         const uint32_t *__restrict__ large_ord,
-                                        const uint32_t *__restrict__ totals) {
+                                        const uint32_t *__restrict__ totals, const uint32_t *__restrict__ tile_seg) {
   constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
   const uint32_t t = blockIdx.x;
   if (t >= totals[0]) return;
-  const LargeTile lt = locate_tile<U>(offsets, tile_first, large_ord, nseg, t, TILE);
+  const LargeTile lt = tile_of_segment(offsets, tile_first, large_ord, tile_seg[t], t, TILE);
   for (uint32_t i = threadIdx.x; i < lt.count; i += blockDim.x) {
     keys_main[lt.base + i] = keys_alt[lt.base + i];
     if (VB) vals_main[lt.base + i] = vals_alt[lt.base + i];
@@ -366,7 +373,7 @@ segsort_small_kernel(U *__restrict__ keys, typename value_type_of<VB>::type *__r
 
 // ---- host ------------------------------------------------------------------
 struct SegLayout {
-  size_t alt_keys, alt_vals, tile_first, large_ord, seg_of_large, totals, counters, seg_hist, status, total;
+  size_t alt_keys, alt_vals, tile_first, large_ord, seg_of_large, tile_seg, totals, counters, seg_hist, status, total;
   size_t zero_begin, zero_bytes;
   uint32_t max_tiles, max_large;
 };
@@ -392,6 +399,8 @@ SegLayout seg_layout(size_t n, size_t nseg) {
   off += align256(nseg * 4);
   L.seg_of_large = off;
   off += align256(nseg * 4);
+  L.tile_seg = off;
+  off += align256(size_t(L.max_tiles) * 4);
   L.totals = off;
   off += 256;
   L.counters = off;  // small-segment ticket + one ticket per pass
@@ -456,6 +465,7 @@ bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const u
   uint32_t *tile_first = reinterpret_cast<uint32_t *>(base + L.tile_first);
   uint32_t *large_ord = reinterpret_cast<uint32_t *>(base + L.large_ord);
   uint32_t *seg_of_large = reinterpret_cast<uint32_t *>(base + L.seg_of_large);
+  uint32_t *tile_seg = reinterpret_cast<uint32_t *>(base + L.tile_seg);
   uint32_t *totals = reinterpret_cast<uint32_t *>(base + L.totals);
   uint32_t *counters = reinterpret_cast<uint32_t *>(base + L.counters);
   uint32_t *seg_hist = reinterpret_cast<uint32_t *>(base + L.seg_hist);
@@ -481,7 +491,7 @@ bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const u
   {
     KernelScope ks("segsort_hist", s);
     segsort_hist_kernel<U, PASSES><<<L.max_tiles, kHistThreads, 0, s>>>(
-        k_main, offsets, uint32_t(nseg), tile_first, large_ord, totals, TILE, xf, seg_hist);
+        k_main, offsets, uint32_t(nseg), tile_first, large_ord, totals, TILE, xf, seg_hist, tile_seg);
     rc = launch_status("segsort_hist");
     if (rc) return rc;
   }
@@ -502,14 +512,15 @@ bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const u
     KernelScope ks("segsort_onesweep", s);
     segsort_onesweep_kernel<U, VB><<<L.max_tiles, kSortThreads, smem, s>>>(
         k_main, k_alt, v_main, v_alt, uint32_t(n), offsets, uint32_t(nseg), tile_first, large_ord, totals, p,
-        PASSES, xf, seg_hist, status + size_t(p) * L.max_tiles * kRadix, counters + 1 + p, ds->err_word);
+        PASSES, xf, seg_hist, status + size_t(p) * L.max_tiles * kRadix, counters + 1 + p, tile_seg, ds->err_word);
     rc = launch_status("segsort_onesweep");
     if (rc) return rc;
   }
   if (PASSES & 1) {
     KernelScope ks("segsort_copyback", s);
     segsort_copyback_kernel<U, VB><<<L.max_tiles, 256, 0, s>>>(k_main, k_alt, v_main, v_alt, offsets,
-                                                               uint32_t(nseg), tile_first, large_ord, totals);
+                                                               uint32_t(nseg), tile_first, large_ord, totals,
+                                                               tile_seg);
     rc = launch_status("segsort_copyback");
   }
   return rc;

@@ -447,6 +447,9 @@ bcx_status bcx_sort_pairs_host(bcx_stream stream, bcx_dtype key_type, size_t val
   BCX_CHECK(dtype_valid(key_type), BCX_INVALID_VALUE, "invalid key dtype %d", int(key_type));
   if (n == 0) return BCX_SUCCESS;
   cudaStream_t s = (cudaStream_t)stream;
+  DeviceState *ds = nullptr;
+  bcx_status rc = current_device_state(&ds);
+  if (rc) return rc;
   const size_t kb = n * dtype_size(key_type), vb = n * value_bytes;
   void *dk = nullptr, *dv = nullptr;
   BCX_CUDA(cudaMallocAsync(&dk, kb, s));
@@ -457,23 +460,46 @@ bcx_status bcx_sort_pairs_host(bcx_stream stream, bcx_dtype key_type, size_t val
       return cuda_status(e, "cudaMallocAsync(values)");
     }
   }
-  bcx_status rc = BCX_SUCCESS;
-  cudaError_t e = cudaMemcpyAsync(dk, host_keys, kb, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && vb) e = cudaMemcpyAsync(dv, host_values, vb, cudaMemcpyHostToDevice, s);
+  // Each direction's copies are split over the caller's stream and the
+  // library's second stream (keys on one, values on the other; keys-only
+  // sorts split the keys in halves), so two copy engines share the link.
+  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+  cudaStream_t s2 = ds->aux_stream;
+  char *hk = static_cast<char *>(host_keys), *hv = static_cast<char *>(host_values);
+  char *dkc = static_cast<char *>(dk), *dvc = static_cast<char *>(dv);
+  const size_t khalf = vb ? kb : (kb / 2) & ~size_t(255);
+  auto split_copy = [&](cudaMemcpyKind kind) -> cudaError_t {
+    cudaError_t r = cudaEventRecord(fork, s);
+    if (r == cudaSuccess) r = cudaStreamWaitEvent(s2, fork, 0);
+    const bool h2d = kind == cudaMemcpyHostToDevice;
+    if (r == cudaSuccess)
+      r = h2d ? cudaMemcpyAsync(dkc, hk, khalf, kind, s) : cudaMemcpyAsync(hk, dkc, khalf, kind, s);
+    if (r == cudaSuccess && kb > khalf)
+      r = h2d ? cudaMemcpyAsync(dkc + khalf, hk + khalf, kb - khalf, kind, s2)
+              : cudaMemcpyAsync(hk + khalf, dkc + khalf, kb - khalf, kind, s2);
+    if (r == cudaSuccess && vb) r = h2d ? cudaMemcpyAsync(dvc, hv, vb, kind, s2) : cudaMemcpyAsync(hv, dvc, vb, kind, s2);
+    if (r == cudaSuccess) r = cudaEventRecord(join, s2);
+    if (r == cudaSuccess) r = cudaStreamWaitEvent(s, join, 0);
+    return r;
+  };
+  if (e == cudaSuccess) e = split_copy(cudaMemcpyHostToDevice);
   if (e != cudaSuccess) rc = cuda_status(e, "copy to device");
   if (!rc) {
     rc = vb ? bcx_sort_pairs(stream, key_type, value_bytes, dk, dv, n, descending, nullptr, nullptr)
             : bcx_sort_keys(stream, key_type, dk, n, descending, nullptr, nullptr);
   }
   if (!rc) {
-    e = cudaMemcpyAsync(host_keys, dk, kb, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && vb) e = cudaMemcpyAsync(host_values, dv, vb, cudaMemcpyDeviceToHost, s);
+    e = split_copy(cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) rc = cuda_status(e, "copy to host");
   }
   cudaFreeAsync(dk, s);
   if (dv) cudaFreeAsync(dv, s);
   e = cudaStreamSynchronize(s);
   if (!rc && e != cudaSuccess) rc = cuda_status(e, "cudaStreamSynchronize");
+  if (fork) cudaEventDestroy(fork);
+  if (join) cudaEventDestroy(join);
   return rc;
 }
 
