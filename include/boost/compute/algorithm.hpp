@@ -2,6 +2,12 @@
 #ifndef BOOST_COMPUTE_ALGORITHM_HPP
 #define BOOST_COMPUTE_ALGORITHM_HPP
 #include <boost/compute/algorithm/copy.hpp>
+#include <boost/compute/algorithm/copy_if.hpp>
+#include <boost/compute/algorithm/count.hpp>
+#include <boost/compute/algorithm/count_if.hpp>
+#include <boost/compute/algorithm/inner_product.hpp>
+#include <boost/compute/algorithm/max_element.hpp>
+#include <boost/compute/algorithm/min_element.hpp>
 #include <boost/compute/algorithm/reduce.hpp>
 #include <boost/compute/algorithm/reduce_by_key.hpp>
 #include <boost/compute/algorithm/scan.hpp>

@@ -33,8 +33,9 @@ inline typename std::enable_if<is_jit_functor<G>::value>::type functor_expr(cons
   *e = g.print();
 }
 template <class G>
-inline typename std::enable_if<!is_jit_functor<G>::value && is_builtin_binary<G>::value>::type functor_expr(
-    const G &, std::string *d, std::string *e) {
+inline typename std::enable_if<!is_jit_functor<G>::value &&
+                               (is_builtin_binary<G>::value || is_builtin_compare<G>::value)>::type
+functor_expr(const G &, std::string *d, std::string *e) {
   const std::string s = G::source();  // spelled with a and b
   d->clear();
   e->clear();
@@ -45,14 +46,17 @@ inline typename std::enable_if<!is_jit_functor<G>::value && is_builtin_binary<G>
   }
 }
 template <class G>
-inline typename std::enable_if<!is_jit_functor<G>::value && !is_builtin_binary<G>::value>::type functor_expr(
-    const G &, std::string *d, std::string *e) {
+inline typename std::enable_if<!is_jit_functor<G>::value && !is_builtin_binary<G>::value &&
+                               !is_builtin_compare<G>::value>::type
+functor_expr(const G &, std::string *d, std::string *e) {
   d->clear();
   *e = builtin_unary_expr<G>();
 }
 
+// out = [init op] fold(op, f(a[i] [, b[i]])), one generated kernel.
 template <class T, class A, class B, class F, class Op>
-inline void fused_transform_reduce(const A *a, const B *b, size_t n, F f, Op op, T *out, command_queue &queue) {
+inline void fused_transform_reduce(const A *a, const B *b, size_t n, F f, Op op, T *out, command_queue &queue,
+                                   const T *init = nullptr) {
   std::string fd, fe, od, oe;
   functor_expr(f, &fd, &fe);
   functor_expr(op, &od, &oe);
@@ -60,7 +64,7 @@ inline void fused_transform_reduce(const A *a, const B *b, size_t n, F f, Op op,
   if (b) load += "const auto _2 = b[i]; ";
   load += "return (T)(" + fe + ");";
   jit_fold(fd + "\n" + od, oe, cuda_type_name<T>::get(), sizeof(T), load, cuda_type_name<A>::get(),
-           b ? cuda_type_name<B>::get() : nullptr, a, b, n, nullptr, out, queue);
+           b ? cuda_type_name<B>::get() : nullptr, a, b, n, init, out, queue);
 }
 
 }  // namespace detail

@@ -83,6 +83,14 @@ template <class T> struct is_builtin_unary<negate<T> > { static const bool value
 template <class T> struct is_builtin_unary<abs<T> > { static const bool value = true; };
 template <class T> struct is_builtin_unary<sqrt<T> > { static const bool value = true; };
 template <class T> struct is_builtin_unary<logical_not<T> > { static const bool value = true; };
+// Comparisons, spelled with a and b like the binary functors.
+template <class F> struct is_builtin_compare { static const bool value = false; };
+template <class T> struct is_builtin_compare<less<T> > { static const bool value = true; };
+template <class T> struct is_builtin_compare<greater<T> > { static const bool value = true; };
+template <class T> struct is_builtin_compare<equal_to<T> > { static const bool value = true; };
+template <class T> struct is_builtin_compare<not_equal_to<T> > { static const bool value = true; };
+template <class T> struct is_builtin_compare<less_equal<T> > { static const bool value = true; };
+template <class T> struct is_builtin_compare<greater_equal<T> > { static const bool value = true; };
 }  // namespace detail
 
 }  // namespace compute

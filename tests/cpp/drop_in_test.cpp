@@ -288,6 +288,62 @@ static void transform_reduce_cases(compute::command_queue &q) {
   CHECK(r1.begin().read(q) == (-500 - 0) + (-499 - 7) + (-498 - 14) + (-497 - 21));
 }
 
+static void scan_family_cases(compute::command_queue &q) {
+  using compute::_1;
+  using compute::_2;
+  // test/test_count.cpp (count / count_if with a lambda)
+  int cd[] = {1, 2, 1, 2, 3, 1, 4, 1};
+  compute::vector<int> cv(cd, cd + 8, q);
+  CHECK(compute::count(cv.begin(), cv.end(), 1, q) == 4);
+  CHECK(compute::count(cv.begin(), cv.end(), 5, q) == 0);
+  CHECK(compute::count_if(cv.begin(), cv.end(), _1 > 1, q) == 4);
+  BOOST_COMPUTE_FUNCTION(bool, is_odd, (int x), { return x & 1; });
+  CHECK(compute::count_if(cv.begin(), cv.end(), is_odd, q) == 5);
+  // a large count: 2^20 + 5 elements, every third one matches
+  const size_t n = (1 << 20) + 5;
+  std::vector<int> big(n);
+  for (size_t i = 0; i < n; ++i) big[i] = int(i % 3);
+  compute::vector<int> bv(big.begin(), big.end(), q);
+  CHECK(compute::count(bv.begin(), bv.end(), 0, q) == (n + 2) / 3);
+  // inner_product (test/test_inner_product.cpp)
+  int ad[] = {1, 2, 3, 4}, bd[] = {5, 6, 7, 8};
+  compute::vector<int> a(ad, ad + 4, q), b(bd, bd + 4, q);
+  CHECK(compute::inner_product(a.begin(), a.end(), b.begin(), 10, q) == 10 + 70);
+  CHECK(compute::inner_product(a.begin(), a.end(), b.begin(), 0, compute::plus<int>(), compute::minus<int>(), q) == -16);
+  // min_element / max_element return the FIRST extremum (test/test_extrema.cpp)
+  int ed[] = {9, 15, 1, 4, 1, 15, 9, 0, 0, 12};
+  compute::vector<int> ev(ed, ed + 10, q);
+  CHECK(compute::min_element(ev.begin(), ev.end(), q) - ev.begin() == 7);
+  CHECK(compute::max_element(ev.begin(), ev.end(), q) - ev.begin() == 1);
+  CHECK(compute::min_element(ev.begin(), ev.end(), compute::greater<int>(), q) - ev.begin() == 1);
+  CHECK(compute::max_element(ev.begin(), ev.end(), _1 > _2, q) - ev.begin() == 7);
+  std::vector<float> fx(n);
+  for (size_t i = 0; i < n; ++i) fx[i] = float((i * 7919) % 100003);
+  fx[123457] = -5.f;
+  fx[999999] = -5.f;
+  fx[54321] = 200000.f;
+  compute::vector<float> fv(fx.begin(), fx.end(), q);
+  CHECK(compute::min_element(fv.begin(), fv.end(), q) - fv.begin() == 123457);
+  CHECK(compute::max_element(fv.begin(), fv.end(), q) - fv.begin() == 54321);
+  // copy_if / remove_copy_if keep order (test/test_copy_if.cpp)
+  int xd[] = {1, 6, 2, 7, 3, 8, 4, 9, 5};
+  compute::vector<int> xv(xd, xd + 9, q), out(9, q.get_context());
+  auto end = compute::copy_if(xv.begin(), xv.end(), out.begin(), _1 > 4, q);
+  CHECK(end - out.begin() == 5);
+  std::vector<int> ho = to_host(out, q);
+  CHECK((std::vector<int>(ho.begin(), ho.begin() + 5) == std::vector<int>{6, 7, 8, 9, 5}));
+  end = compute::remove_copy_if(xv.begin(), xv.end(), out.begin(), _1 > 4, q);
+  ho = to_host(out, q);
+  CHECK(end - out.begin() == 4 && (std::vector<int>(ho.begin(), ho.begin() + 4) == std::vector<int>{1, 2, 3, 4}));
+  compute::vector<int> bo(n, q.get_context());
+  auto bend = compute::copy_if(bv.begin(), bv.end(), bo.begin(), _1 == 2, q);
+  CHECK(size_t(bend - bo.begin()) == n / 3);
+  std::vector<int> hb = to_host(bo, q);
+  bool all2 = true;
+  for (size_t i = 0; i < n / 3; ++i) all2 = all2 && hb[i] == 2;
+  CHECK(all2);
+}
+
 static void error_cases(compute::command_queue &q) {
   // bcx errors surface as opencl_error with the OpenCL status code
   bool thrown = false;
@@ -310,6 +366,7 @@ int main() {
   reduce_by_key_cases(q);
   jit_cases(q);
   transform_reduce_cases(q);
+  scan_family_cases(q);
   error_cases(q);
   q.check_device_errors();
   std::printf("%s (%d failures)\n", g_failures ? "FAILED" : "OK", g_failures);
