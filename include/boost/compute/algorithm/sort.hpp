@@ -15,7 +15,9 @@
 #include <vector>
 
 #include <boost/compute/algorithm/copy.hpp>
+#include <boost/compute/detail/merge_sort.hpp>
 #include <boost/compute/functional.hpp>
+#include <boost/compute/iterator/transform_iterator.hpp>
 
 namespace boost {
 namespace compute {
@@ -41,9 +43,19 @@ inline void device_sort_by_key(buffer_iterator<K> kf, buffer_iterator<K> kl, buf
 }  // namespace detail
 
 template <class T, class Compare>
-inline void sort(buffer_iterator<T> first, buffer_iterator<T> last, Compare compare,
-                 command_queue &queue = system::default_queue()) {
+inline typename std::enable_if<!detail::is_jit_functor<Compare>::value>::type
+sort(buffer_iterator<T> first, buffer_iterator<T> last, Compare compare,
+     command_queue &queue = system::default_queue()) {
   detail::device_sort(first, last, detail::sort_direction(compare), queue);
+}
+// A lambda or BOOST_COMPUTE_FUNCTION comparator: the generated stable merge
+// sort (detail/merge_sort.hpp).
+template <class T, class Compare>
+inline typename std::enable_if<detail::is_jit_functor<Compare>::value>::type
+sort(buffer_iterator<T> first, buffer_iterator<T> last, Compare compare,
+     command_queue &queue = system::default_queue()) {
+  detail::jit_merge_sort<T, unsigned char>(first.get_ptr(), nullptr, size_t(last - first), compare.defs(),
+                                           compare.print(), queue);
 }
 template <class T>
 inline void sort(buffer_iterator<T> first, buffer_iterator<T> last, command_queue &queue = system::default_queue()) {
@@ -66,9 +78,16 @@ sort(Iterator first, Iterator last, command_queue &queue = system::default_queue
 }
 
 template <class K, class V, class Compare>
-inline void sort_by_key(buffer_iterator<K> kf, buffer_iterator<K> kl, buffer_iterator<V> vf, Compare compare,
-                        command_queue &queue = system::default_queue()) {
+inline typename std::enable_if<!detail::is_jit_functor<Compare>::value>::type
+sort_by_key(buffer_iterator<K> kf, buffer_iterator<K> kl, buffer_iterator<V> vf, Compare compare,
+            command_queue &queue = system::default_queue()) {
   detail::device_sort_by_key(kf, kl, vf, detail::sort_direction(compare), queue);
+}
+template <class K, class V, class Compare>
+inline typename std::enable_if<detail::is_jit_functor<Compare>::value>::type
+sort_by_key(buffer_iterator<K> kf, buffer_iterator<K> kl, buffer_iterator<V> vf, Compare compare,
+            command_queue &queue = system::default_queue()) {
+  detail::jit_merge_sort<K, V>(kf.get_ptr(), vf.get_ptr(), size_t(kl - kf), compare.defs(), compare.print(), queue);
 }
 template <class K, class V>
 inline void sort_by_key(buffer_iterator<K> kf, buffer_iterator<K> kl, buffer_iterator<V> vf,

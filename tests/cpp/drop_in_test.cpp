@@ -344,6 +344,44 @@ static void scan_family_cases(compute::command_queue &q) {
   CHECK(all2);
 }
 
+static void comparator_sort_cases(compute::command_queue &q) {
+  using compute::_1;
+  using compute::_2;
+  // test/test_sort.cpp: sort with a lambda comparator (descending)
+  int d[] = {3, 9, -1, 4, 4, 0, 7};
+  compute::vector<int> v(d, d + 7, q);
+  compute::sort(v.begin(), v.end(), _1 > _2, q);
+  CHECK((to_host(v, q) == std::vector<int>{9, 7, 4, 4, 3, 0, -1}));
+  // stable_sort_by_key with a user comparator on |key|: ties keep input order
+  BOOST_COMPUTE_FUNCTION(bool, abs_less, (int a, int b), { return abs(a) < abs(b); });
+  const size_t n = (1 << 20) + 3;
+  std::mt19937 gen(7);
+  std::uniform_int_distribution<int> dist(-5000, 5000);
+  std::vector<int> hk(n), hv(n);
+  for (size_t i = 0; i < n; ++i) {
+    hk[i] = dist(gen);
+    hv[i] = int(i);
+  }
+  compute::vector<int> k(hk.begin(), hk.end(), q), val(hv.begin(), hv.end(), q);
+  compute::stable_sort_by_key(k.begin(), k.end(), val.begin(), abs_less, q);
+  std::vector<size_t> idx(n);
+  for (size_t i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return std::abs(hk[a]) < std::abs(hk[b]); });
+  std::vector<int> gk = to_host(k, q), gv = to_host(val, q);
+  bool same = true;
+  for (size_t i = 0; i < n; ++i) same = same && gk[i] == hk[idx[i]] && gv[i] == int(idx[i]);
+  CHECK(same);
+  // keys only, float, lambda comparator, 3 * 2^18 + 5 elements
+  const size_t m = 3 * (1 << 18) + 5;
+  std::vector<float> hf(m);
+  std::uniform_real_distribution<float> u(-1.f, 1.f);
+  for (size_t i = 0; i < m; ++i) hf[i] = u(gen);
+  compute::vector<float> fv(hf.begin(), hf.end(), q);
+  compute::sort(fv.begin(), fv.end(), _1 < _2, q);
+  std::sort(hf.begin(), hf.end());
+  CHECK(to_host(fv, q) == hf);
+}
+
 static void error_cases(compute::command_queue &q) {
   // bcx errors surface as opencl_error with the OpenCL status code
   bool thrown = false;
@@ -367,6 +405,7 @@ int main() {
   jit_cases(q);
   transform_reduce_cases(q);
   scan_family_cases(q);
+  comparator_sort_cases(q);
   error_cases(q);
   q.check_device_errors();
   std::printf("%s (%d failures)\n", g_failures ? "FAILED" : "OK", g_failures);
