@@ -42,6 +42,7 @@ struct RbPlain {
   __device__ __forceinline__ static Acc ident() { return Op::identity(); }
   __device__ __forceinline__ static Acc from(V x) { return Acc(x); }
   __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return Op()(a, b); }
+  __device__ __forceinline__ static Acc add1(Acc a, V x) { return Op()(a, Acc(x)); }
   __device__ __forceinline__ static V out(Acc a) { return V(a); }
   __device__ __forceinline__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
   __device__ __forceinline__ static Acc shfl_down(Acc a, int d) { return __shfl_down_sync(0xffffffffu, a, d); }
@@ -52,6 +53,7 @@ struct RbCompF32 {
   __device__ __forceinline__ static Acc ident() { return comp_f32{0.f, 0.f}; }
   __device__ __forceinline__ static Acc from(float x) { return comp_f32{x, 0.f}; }
   __device__ __forceinline__ static Acc comb(Acc a, Acc b) { return comp_merge(a, b); }
+  __device__ __forceinline__ static Acc add1(Acc a, float x) { return comp_add(a, x); }
   __device__ __forceinline__ static float out(Acc a) { return a.s + a.c; }
   __device__ __forceinline__ static Acc shfl_up(Acc a, int d) {
     return comp_f32{__shfl_up_sync(0xffffffffu, a.s, d), __shfl_up_sync(0xffffffffu, a.c, d)};
@@ -80,6 +82,18 @@ __device__ __forceinline__ Seg<P> seg_comb(const Seg<P> &a, const Seg<P> &b) {
 template <class P>
 __device__ __forceinline__ Seg<P> seg_ident() {
   return Seg<P>{0u, P::ident()};
+}
+
+// a then one element x: a head restarts the run with x (and counts a run),
+// otherwise x is folded into the running value.
+template <class P, class V>
+__device__ __forceinline__ void seg_push(Seg<P> &a, bool head, V x) {
+  if (head) {
+    a.c = ((a.c & kCountMask) + 1u) | kHeadBit;
+    a.v = P::from(x);
+  } else {
+    a.v = P::add1(a.v, x);
+  }
 }
 
 template <class P>
@@ -163,45 +177,31 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   // owns elements chunk_base + l*N .. + N-1, so (j, l, m) is input order.
   const size_t warp_base = size_t(tile) * Sh::TILE + size_t(warp) * (CH * kWarp * N);
 
-  K k[CH][N];
-  V v[CH][N];
-#pragma unroll
-  for (int j = 0; j < CH; ++j) {
-    const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
-    load_run<K, N>(keys, e0, n, vec_k != 0, k[j]);
-    load_run<V, N>(vals, e0, n, vec_v != 0, v[j]);
-  }
-  // Head flags: bit j*N+m = element (j, m) starts a run.
-  uint32_t heads = 0;
-  const K before = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);
-#pragma unroll
-  for (int j = 0; j < CH; ++j) {
-    const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
-    K prev = __shfl_up_sync(0xffffffffu, k[j][N - 1], 1);
-    const K last_prev_chunk = __shfl_sync(0xffffffffu, k[j > 0 ? j - 1 : 0][N - 1], kWarp - 1);
-    if (lane == 0) prev = j > 0 ? last_prev_chunk : before;
-#pragma unroll
-    for (int m = 0; m < N; ++m) {
-      const size_t idx = e0 + m;
-      const K p = m > 0 ? k[j][m - 1] : prev;
-      const bool h = idx < n && (idx == 0 || !keys_equal(p, k[j][m]));
-      heads |= uint32_t(h) << (j * N + m);
-    }
-  }
-  // Per chunk: serial fold of the lane's N elements, warp scan of the lane
-  // folds, carried across chunks.
-  S lane_excl[CH], chunk_pre[CH];
+  // Pass 1 over the tile: head flags and per-chunk prefixes.  Only those stay
+  // in registers across the look-back; pass 2 reads the keys and values again
+  // (they were read microseconds earlier, so from L2) to emit the results.
+  uint32_t heads = 0;  // bit j*N+m = element (j, m) starts a run
+  S lane_pre[CH];      // fold of everything before the lane's run in chunk j (within the warp)
   S run = seg_ident<P>();
+  K carry_key = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);  // key before chunk j
 #pragma unroll
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
+    K k[N];
+    V v[N];
+    load_run<K, N>(keys, e0, n, vec_k != 0, k);
+    load_run<V, N>(vals, e0, n, vec_v != 0, v);
+    K prev = __shfl_up_sync(0xffffffffu, k[N - 1], 1);
+    if (lane == 0) prev = carry_key;
+    carry_key = __shfl_sync(0xffffffffu, k[N - 1], kWarp - 1);
     S a = seg_ident<P>();
 #pragma unroll
     for (int m = 0; m < N; ++m) {
-      S e;
-      e.c = ((heads >> (j * N + m)) & 1u) ? (kHeadBit | 1u) : 0u;
-      e.v = (e0 + m < n) ? P::from(v[j][m]) : P::ident();
-      a = seg_comb<P>(a, e);
+      const size_t idx = e0 + m;
+      const K p = m > 0 ? k[m - 1] : prev;
+      const bool h = idx < n && (idx == 0 || !keys_equal(p, k[m]));
+      heads |= uint32_t(h) << (j * N + m);
+      if (idx < n) seg_push<P>(a, h, v[m]);
     }
     S x = a;
 #pragma unroll
@@ -214,8 +214,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
     S ex;
     ex.c = __shfl_up_sync(0xffffffffu, x.c, 1);
     ex.v = P::shfl_up(x.v, 1);
-    lane_excl[j] = lane == 0 ? seg_ident<P>() : ex;
-    chunk_pre[j] = run;
+    lane_pre[j] = lane == 0 ? run : seg_comb<P>(run, ex);
     S tot;
     tot.c = __shfl_sync(0xffffffffu, x.c, kWarp - 1);
     tot.v = P::shfl(x.v, kWarp - 1);
@@ -281,31 +280,32 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
     if (lane == 0) s_prefix = excl;
   }
   __syncthreads();
-  // Emit: run heads write their key, run ends their reduced value.
+  // Pass 2: run heads write their key, run ends their reduced value.
   const S pre = seg_comb<P>(s_prefix, warp_excl);
   const size_t warp_end = warp_base + size_t(CH) * kWarp * N;  // first element after this warp
-  const bool after_head = warp_end < n && !keys_equal(k[CH - 1][N - 1], lane == kWarp - 1 ? keys[warp_end] : k[CH - 1][N - 1]);
+  const bool after_head = lane == kWarp - 1 && warp_end < n && !keys_equal(keys[warp_end], carry_key);
 #pragma unroll
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
+    K k[N];
+    V v[N];
+    load_run<K, N>(keys, e0, n, vec_k != 0, k);
+    load_run<V, N>(vals, e0, n, vec_v != 0, v);
     // head flag of the element after this lane's run in chunk j
     const uint32_t h_next_lane = __shfl_down_sync(0xffffffffu, heads >> (j * N), 1) & 1u;
     const uint32_t h_next_chunk = __shfl_sync(0xffffffffu, heads >> (j + 1 < CH ? (j + 1) * N : 0), 0) & 1u;
     uint32_t next_h = h_next_lane;
     if (lane == kWarp - 1) next_h = j + 1 < CH ? h_next_chunk : uint32_t(after_head);
-    S acc = seg_comb<P>(seg_comb<P>(pre, chunk_pre[j]), lane_excl[j]);
+    S acc = seg_comb<P>(pre, lane_pre[j]);
 #pragma unroll
     for (int m = 0; m < N; ++m) {
       const size_t idx = e0 + m;
       const bool h = (heads >> (j * N + m)) & 1u;
-      S e;
-      e.c = h ? (kHeadBit | 1u) : 0u;
-      e.v = idx < n ? P::from(v[j][m]) : P::ident();
-      acc = seg_comb<P>(acc, e);
       if (idx < n) {
+        seg_push<P>(acc, h, v[m]);
         const uint32_t run_idx = (acc.c & kCountMask) - 1u;
         const bool last = idx + 1 == n || (m + 1 < N ? ((heads >> (j * N + m + 1)) & 1u) != 0 : next_h != 0);
-        if (h && keys_out) keys_out[run_idx] = k[j][m];
+        if (h && keys_out) keys_out[run_idx] = k[m];
         if (last) vals_out[run_idx] = P::out(acc.v);
         if (idx + 1 == n) *num_runs = (unsigned long long)(acc.c & kCountMask);
       }

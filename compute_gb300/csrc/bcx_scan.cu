@@ -273,9 +273,31 @@ __device__ __forceinline__ void load_chunk(const T *__restrict__ in, size_t vi, 
   }
 }
 
+// First read of a chunk: cached in L2 (not L1) so that the second read after
+// the look-back hits L2.
+template <class T>
+__device__ __forceinline__ void load_chunk_l2(const T *__restrict__ in, size_t vi, size_t head_pad,
+                                              size_t nv, bool vec_ok, T (&x)[16 / sizeof(T)]) {
+  constexpr int N = 16 / sizeof(T);
+  const size_t u0 = vi * N;
+  if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
+    uint4 u = __ldcg(reinterpret_cast<const uint4 *>(reinterpret_cast<const vec16<T> *>(in - head_pad) + vi));
+    vec16<T> r;
+    memcpy(&r, &u, 16);
+#pragma unroll
+    for (int k = 0; k < N; ++k) x[k] = r.v[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const size_t u = u0 + k;
+      x[k] = (u >= head_pad && u < nv) ? in[u - head_pad] : T(0);
+    }
+  }
+}
+
 // One block = one tile of THREADS * V vectors.
 template <class T, class P, int THREADS, int V, bool SINGLE, class Status>
-__global__ void __launch_bounds__(THREADS)
+__global__ void __launch_bounds__(THREADS, (THREADS >= 256 ? 4 : 8))
 scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t head_pad,
                  int vec_ok, int exclusive, typename P::Carry init_carry, Status st,
                  uint32_t *tile_counter, uint32_t *err) {
@@ -299,31 +321,34 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   const size_t tile_vec0 = tile * size_t(THREADS) * V;
   const size_t warp_vec0 = tile_vec0 + size_t(warp) * kWarp * V;
 
-  T x[V][N];
+  constexpr int G = (16 / N) < V ? (16 / N) : V;  // chunks loaded together (16 elements)
   Acc lane_pre[V];  // prefix of this lane's first element within the warp's part of the tile
   Acc run = P::ident();
-  // element (j, k) lies in [head_pad, nv): the tile's interior is always
-  // in range, only the array's first and last tiles test it
   const bool interior = (warp_vec0 * N >= head_pad) && (warp_vec0 + size_t(V) * kWarp) * N <= nv;
 #pragma unroll
-  for (int j = 0; j < V; ++j) load_chunk<T>(in, warp_vec0 + size_t(j) * kWarp + lane, head_pad, nv, vec_ok != 0, x[j]);
+  for (int g = 0; g < V; g += G) {
+    T x[G][N];
 #pragma unroll
-  for (int j = 0; j < V; ++j) {
-    const size_t u0 = (warp_vec0 + size_t(j) * kWarp + lane) * N;
-    Acc t = P::ident();
+    for (int c = 0; c < G; ++c)
+      load_chunk_l2<T>(in, warp_vec0 + size_t(g + c) * kWarp + lane, head_pad, nv, vec_ok != 0, x[c]);
 #pragma unroll
-    for (int k = 0; k < N; ++k)
-      if (interior || (u0 + k >= head_pad && u0 + k < nv)) t = P::add(t, x[j][k]);
-    // inclusive warp scan of the per-lane totals of chunk j
-    Acc incl = t;
+    for (int c = 0; c < G; ++c) {
+      const int j = g + c;
+      const size_t u0 = (warp_vec0 + size_t(j) * kWarp + lane) * N;
+      Acc t = P::ident();
 #pragma unroll
-    for (int d = 1; d < kWarp; d <<= 1) {
-      Acc o = P::shfl_up(incl, d);
-      if (int(lane) >= d) incl = P::comb(o, incl);
+      for (int k = 0; k < N; ++k)
+        if (interior || (u0 + k >= head_pad && u0 + k < nv)) t = P::add(t, x[c][k]);
+      Acc incl = t;
+#pragma unroll
+      for (int d = 1; d < kWarp; d <<= 1) {
+        Acc o = P::shfl_up(incl, d);
+        if (int(lane) >= d) incl = P::comb(o, incl);
+      }
+      Acc ex = P::shfl_up(incl, 1);
+      lane_pre[j] = (lane == 0) ? run : P::comb(run, ex);
+      run = P::comb(run, P::shfl(incl, kWarp - 1));
     }
-    Acc ex = P::shfl_up(incl, 1);
-    lane_pre[j] = (lane == 0) ? run : P::comb(run, ex);
-    run = P::comb(run, P::shfl(incl, kWarp - 1));
   }
   if (lane == 0) warp_tot[warp] = run;
   __syncthreads();
@@ -352,31 +377,39 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   const Acc base = P::comb(P::from_carry(tile_prefix), warp_excl);
   T *vout_base = out - head_pad;
 #pragma unroll
-  for (int j = 0; j < V; ++j) {
-    const size_t vi = warp_vec0 + size_t(j) * kWarp + lane;
-    const size_t u0 = vi * N;
-    Acc r = P::comb(base, lane_pre[j]);
-    T y[N];
+  for (int g = 0; g < V; g += G) {
+    T x[G][N];
 #pragma unroll
-    for (int k = 0; k < N; ++k) {
-      const bool ok = interior || (u0 + k >= head_pad && u0 + k < nv);
-      if (exclusive) {
-        y[k] = P::out(r);
-        if (ok) r = P::add(r, x[j][k]);
-      } else {
-        if (ok) r = P::add(r, x[j][k]);
-        y[k] = P::out(r);
+    for (int c = 0; c < G; ++c)
+      load_chunk<T>(in, warp_vec0 + size_t(g + c) * kWarp + lane, head_pad, nv, vec_ok != 0, x[c]);
+#pragma unroll
+    for (int c = 0; c < G; ++c) {
+      const int j = g + c;
+      const size_t vi = warp_vec0 + size_t(j) * kWarp + lane;
+      const size_t u0 = vi * N;
+      Acc r = P::comb(base, lane_pre[j]);
+      T y[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const bool ok = interior || (u0 + k >= head_pad && u0 + k < nv);
+        if (exclusive) {
+          y[k] = P::out(r);
+          if (ok) r = P::add(r, x[c][k]);
+        } else {
+          if (ok) r = P::add(r, x[c][k]);
+          y[k] = P::out(r);
+        }
       }
-    }
-    if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
-      vec16<T> w;
+      if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
+        vec16<T> w;
 #pragma unroll
-      for (int k = 0; k < N; ++k) w.v[k] = y[k];
-      st_stream16(reinterpret_cast<vec16<T> *>(vout_base) + vi, w);
-    } else {
+        for (int k = 0; k < N; ++k) w.v[k] = y[k];
+        st_stream16(reinterpret_cast<vec16<T> *>(vout_base) + vi, w);
+      } else {
 #pragma unroll
-      for (int k = 0; k < N; ++k)
-        if (u0 + k >= head_pad && u0 + k < nv) vout_base[u0 + k] = y[k];
+        for (int k = 0; k < N; ++k)
+          if (u0 + k >= head_pad && u0 + k < nv) vout_base[u0 + k] = y[k];
+      }
     }
   }
 }
