@@ -4,19 +4,32 @@ One step = one compute::sort_by_key of 2^28 uint32 keys (uniform 32-bit) with
 uint32 values (iota) -- the large plain-primitive configuration, the one the
 headline "sort Gkeys/s" is quoted on.  Every step sorts its own freshly
 generated buffer (2 GiB per step, far larger than the 129 MB L2, so no flush
-is needed).  The same run also times the other primitives of that
-configuration (exclusive_scan and reduce of 2^30 int32 in [0,100), transform
-saxpy a=2.5 over 2^28 float32 U[-1,1]) and reports them under "primitives".
+is needed).  The same run reports, in sections of the JSON line:
 
-Prints ONE JSON line (rank 0).  `value` is device throughput with inputs
-resident in HBM; `e2e` is the same metric through the C ABI host-buffer entry
-point (bcx_sort_pairs_host: host->device copy, sort, device->host copy inside
-the timed region); `roofline` is the onesweep pass kernel's algorithmic bytes
-per launch over its average CUDA-event duration inside the timed region;
-`cpu_baseline` is the reference's CPU-device sort (the oracle port of
-merge_sort_by_key_on_cpu) timed on a bounded sample on the host cores.
+  primitives  README float sort of 2^20; exclusive_scan and reduce of 2^30
+              int32 in [0,100); transform saxpy a=2.5 over 2^28 float32 U[-1,1]
+  precision   accumulate / inclusive_scan of 2^30 float32 N(1000,1):
+              compensated vs plain FP32 vs a serial FP32 fold, errors against an
+              FP64 reference; float32 sort of 2^27 with NaN/+-0/denormals/+-inf;
+              uint64 sorts of 2^27 keys (Zipf 1.1, equal, presorted, 8 bits)
+  segmented   10,000 log-uniform segments in [16, 2^20] (and the first 2^28
+              elements of them): segmented sort_by_key, exclusive_scan,
+              reduce_by_key -- autotuned, replayed from a CUDA graph, against one
+              plain call per segment
+  serving     open-loop Poisson arrivals of mixed requests through the
+              continuous-batching server: p50/p99 latency and throughput
+              against serial plain calls
+
+`value` is device throughput with inputs resident in HBM; `e2e` is the same
+metric through the C ABI host-buffer entry point (bcx_sort_pairs_host:
+host->device copy, sort, device->host copy inside the timed region);
+`roofline` is the onesweep pass kernel's algorithmic bytes per launch over its
+average CUDA-event duration inside the timed region; `cpu_baseline` is the
+reference's CPU-device sort (the oracle port of merge_sort_by_key_on_cpu)
+timed on a bounded sample on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--only all|sort|prims|precision|serve|segmented]
 """
 from __future__ import annotations
 

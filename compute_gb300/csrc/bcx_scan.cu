@@ -8,15 +8,22 @@
 //
 // GB300 design: single-pass decoupled look-back.  Each 256-thread block takes
 // the next tile from an atomic ticket (so a block only ever waits on tiles
-// that were handed out before it, which guarantees forward progress), streams
-// its tile with 16-byte loads (warp w owns a contiguous 32*V-vector run; in
-// chunk j lane l owns vector j*32 + l, so every load and store is fully
-// coalesced), scans in registers and warp shuffles, publishes its aggregate,
-// and warp 0 looks back over 32 predecessors at a time for the nearest
-// inclusive prefix.  In-place scans need no copy: a tile reads all of its input
-// before writing any output.  Inputs that fit one tile run as one launch with
-// no look-back.  Every wait on a predecessor is bounded (kSpinLimit polls); on
-// expiry the block records BCX_DEVICE_TIMEOUT and continues.
+// that were handed out before it, which guarantees forward progress) and
+// reads its tile with 16-byte loads (warp w owns a contiguous 32*V-vector run;
+// in chunk j lane l owns vector j*32 + l, so every load and store is fully
+// coalesced).  The first read (cached in L2, not L1) only produces each lane's
+// prefix per chunk by warp shuffles and the tile's aggregate, which is
+// published; warp 0 then looks back over 32 predecessors at a time for the
+// nearest inclusive prefix.  The tile is read a second time for the outputs:
+// it was read microseconds earlier, so that read is served by the 129 MB L2,
+// and keeping no tile data in registers across the look-back lets four 64 KB
+// tiles stay resident per SM, which hides the look-back latency.  DRAM still
+// sees 8 bytes per element.  In-place scans need no copy: a tile reads all of
+// its input (both times) before writing any output -- the second read of a
+// chunk precedes its own write, and other tiles never touch it.  Inputs that
+// fit one tile run as one launch with no look-back.  Every wait on a
+// predecessor is bounded (kSpinLimit polls); on expiry the block records
+// BCX_DEVICE_TIMEOUT and continues.
 //
 // Float plus with compensated=1 keeps Neumaier (s, c) pairs for every sum
 // inside a tile and carries tile prefixes between blocks in FP64.

@@ -32,8 +32,6 @@ namespace {
 
 constexpr int kSegThreads = 256;
 constexpr int kSegWarps = kSegThreads / kWarp;
-constexpr int kSegItems = 8;  // default items per thread of the segmented scan
-constexpr int kSegTile = kSegThreads * kSegItems;  // segmented reduce stride
 enum : uint32_t { kSgInvalid = 0, kSgAggregate = 1, kSgPrefix = 2 };
 
 template <class T, template <class> class OpT>
@@ -92,11 +90,46 @@ __device__ __forceinline__ Sg<P> sg_shfl(const Sg<P> &a, int s) {
   return Sg<P>{__shfl_sync(0xffffffffu, a.h, s), P::shfl(a.v, s)};
 }
 
+// Look-back status of one tile.  With a 4-byte value the flag, the head bit
+// and the value travel in one 64-bit word (relaxed loads and stores suffice);
+// wider values use a flag array plus aggregate/inclusive arrays ordered by
+// release/acquire.
+template <class P, bool PACK = (sizeof(typename P::Acc) == 4)>
+struct SgStatus;
+
 template <class P>
-struct SgStatus {
+struct SgStatus<P, true> {
+  unsigned long long *words;
+  static size_t bytes(size_t tiles) { return align256(tiles * 8); }
+  static size_t zero_bytes(size_t tiles) { return bytes(tiles); }
+  void bind(char *base, size_t) { words = reinterpret_cast<unsigned long long *>(base); }
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, const Sg<P> &v) {
+    uint32_t bits;
+    memcpy(&bits, &v.v, 4);
+    const unsigned long long w = (static_cast<unsigned long long>(bits) << 32) | (v.h << 2) | flag;
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(&words[t]), "l"(w) : "memory");
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, Sg<P> *v) const {
+    const unsigned long long w = ld_relaxed_u64(&words[t]);
+    const uint32_t bits = uint32_t(w >> 32);
+    memcpy(&v->v, &bits, 4);
+    v->h = uint32_t(w >> 2) & 1u;
+    return uint32_t(w & 3u);
+  }
+};
+
+template <class P>
+struct SgStatus<P, false> {
   uint32_t *flags;
   Sg<P> *agg;
   Sg<P> *inc;
+  static size_t bytes(size_t tiles) { return align256(tiles * 4) + 2 * align256(tiles * sizeof(Sg<P>)); }
+  static size_t zero_bytes(size_t tiles) { return align256(tiles * 4); }
+  void bind(char *base, size_t tiles) {
+    flags = reinterpret_cast<uint32_t *>(base);
+    agg = reinterpret_cast<Sg<P> *>(base + align256(tiles * 4));
+    inc = reinterpret_cast<Sg<P> *>(base + align256(tiles * 4) + align256(tiles * sizeof(Sg<P>)));
+  }
   __device__ __forceinline__ void publish(size_t t, uint32_t flag, const Sg<P> &v) {
     if (flag == kSgAggregate) agg[t] = v;
     else inc[t] = v;
@@ -116,28 +149,21 @@ struct SgStatus {
   }
 };
 
-// Index of the first offset >= x among offsets[0..count), found by a whole
-// warp: each step probes 32 evenly spaced entries at once, so 10^4 offsets
-// take three dependent loads instead of fourteen.  Every lane returns the
-// same index.
-__device__ __forceinline__ size_t warp_lower_bound_u64(const unsigned long long *__restrict__ offsets,
-                                                       size_t count, unsigned long long x) {
-  const unsigned lane = lane_id();
-  size_t lo = 0, hi = count;  // the answer lies in [lo, hi]
-  while (hi - lo > size_t(kWarp)) {
-    const size_t step = (hi - lo + kWarp - 1) / kWarp;
-    const size_t p = lo + size_t(lane) * step;
-    const bool ge = p < hi && offsets[p] >= x;
-    const unsigned m = __ballot_sync(0xffffffffu, ge) | __ballot_sync(0xffffffffu, p >= hi);
-    const int f = m ? __ffs(m) - 1 : kWarp;  // first probe at or past the answer
-    if (f == 0) return lo;
-    const size_t below = lo + size_t(f - 1) * step;  // offsets[below] < x
-    hi = (f < kWarp && lo + size_t(f) * step < hi) ? lo + size_t(f) * step : hi;
-    lo = below + 1;
+// First segment whose start is at or after each tile's first element: one
+// thread per tile, so every tile's binary search is in flight at once instead
+// of sitting on the scan kernel's critical path.
+__global__ void seg_tile_first_kernel(const unsigned long long *__restrict__ offsets, size_t nseg, size_t tile,
+                                      size_t tiles, uint32_t *__restrict__ tile_first_seg) {
+  const size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (t >= tiles) return;
+  const unsigned long long x = t * tile;
+  size_t lo = 0, hi = nseg;
+  while (lo < hi) {
+    const size_t mid = (lo + hi) / 2;
+    if (offsets[mid] < x) lo = mid + 1;
+    else hi = mid;
   }
-  const size_t p = lo + lane;
-  const unsigned m = __ballot_sync(0xffffffffu, p < hi && offsets[p] >= x);
-  return m ? lo + size_t(__ffs(m) - 1) : hi;
+  tile_first_seg[t] = uint32_t(lo);
 }
 
 template <class T, int N>
@@ -151,9 +177,9 @@ struct alignas(sizeof(T) * N) SegVec {
 template <class T, class P, int ITEMS>
 __global__ void __launch_bounds__(kSegThreads)
 segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
-                      const unsigned long long *__restrict__ offsets, size_t nseg, int exclusive,
-                      typename P::Acc init, SgStatus<P> st, uint32_t *__restrict__ tile_counter, int vec_in,
-                      int vec_out, uint32_t *err) {
+                      const unsigned long long *__restrict__ offsets, size_t nseg,
+                      const uint32_t *__restrict__ tile_first_seg, int exclusive, typename P::Acc init,
+                      SgStatus<P> st, uint32_t *__restrict__ tile_counter, int vec_in, int vec_out, uint32_t *err) {
   typedef Sg<P> S;
   typedef typename P::Acc Acc;
   constexpr int N = 16 / int(sizeof(T)) < ITEMS ? 16 / int(sizeof(T)) : ITEMS;
@@ -171,24 +197,17 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
   const size_t tile = s_tile;
   const size_t tile_base = tile * TILE;
   const size_t tile_end = (tile_base + TILE < n) ? tile_base + TILE : n;
-  // Mark the segment starts inside this tile (offsets[0..nseg] are starts;
-  // offsets[nseg] == n is not).
-  if (warp == 0) {
-    const size_t first = warp_lower_bound_u64(offsets, nseg, tile_base);
-    for (size_t k = first + lane; k < nseg; k += kWarp) {
-      const unsigned long long o = offsets[k];
-      if (o >= tile_end) break;
-      const uint32_t local = uint32_t(o - tile_base);
-      atomicOr(&s_heads[local >> 5], 1u << (local & 31u));
-    }
-  }
   const uint32_t warp_first = warp * (kWarp * ITEMS);
+  // Pass 1 over the tile: loads first (cached in L2 for the second read), so
+  // they are in flight while warp 0 marks the segment starts.
   T x[CH][N];
 #pragma unroll
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
     if (vec_in && e0 + N <= n) {
-      const SegVec<T, N> w = *reinterpret_cast<const SegVec<T, N> *>(in + e0);
+      const uint4 u = __ldcg(reinterpret_cast<const uint4 *>(in + e0));
+      SegVec<T, N> w;
+      memcpy(&w, &u, sizeof(w));
 #pragma unroll
       for (int m = 0; m < N; ++m) x[j][m] = w.v[m];
     } else {
@@ -196,22 +215,32 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
       for (int m = 0; m < N; ++m) x[j][m] = (e0 + m < n) ? in[e0 + m] : T(0);
     }
   }
-  __syncthreads();
-  uint32_t hb[CH];  // head bits of the lane's run in chunk j (bit m)
-#pragma unroll
-  for (int j = 0; j < CH; ++j) {
-    const uint32_t local = warp_first + j * (kWarp * N) + lane * N;
-    hb[j] = (s_heads[local >> 5] >> (local & 31u)) & ((1u << N) - 1u);
+  // Mark the segment starts inside this tile (offsets[0..nseg] are starts;
+  // offsets[nseg] == n is not).
+  if (warp == 0) {
+    const size_t first = tile_first_seg[tile];
+    for (size_t k = first + lane; k < nseg; k += kWarp) {
+      const unsigned long long o = offsets[k];
+      if (o >= tile_end) break;
+      const uint32_t local = uint32_t(o - tile_base);
+      atomicOr(&s_heads[local >> 5], 1u << (local & 31u));
+    }
   }
-  S lane_excl[CH], chunk_pre[CH];
+  __syncthreads();  // head bitmap complete
+  // Per chunk: serial fold of the lane's run, warp scan of the lane folds.
+  // Only these prefixes stay in registers across the look-back; the tile is
+  // read again (from L2) for the outputs.
+  S lane_pre[CH];  // fold of everything before the lane's run in chunk j (within the warp)
   S run = sg_ident<P>();
 #pragma unroll
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
+    const uint32_t local = warp_first + j * (kWarp * N) + lane * N;
+    const uint32_t hb = (s_heads[local >> 5] >> (local & 31u)) & ((1u << N) - 1u);
     S a = sg_ident<P>();
 #pragma unroll
     for (int m = 0; m < N; ++m) {
-      const S e{(hb[j] >> m) & 1u, (e0 + m < n) ? P::from(x[j][m]) : P::ident()};
+      const S e{(hb >> m) & 1u, (e0 + m < n) ? P::from(x[j][m]) : P::ident()};
       a = sg_comb<P>(a, e);
     }
 #pragma unroll
@@ -220,8 +249,7 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
       if (int(lane) >= d) a = sg_comb<P>(o, a);
     }
     const S ex = sg_shfl_up<P>(a, 1);
-    lane_excl[j] = lane == 0 ? sg_ident<P>() : ex;
-    chunk_pre[j] = run;
+    lane_pre[j] = lane == 0 ? run : sg_comb<P>(run, ex);
     run = sg_comb<P>(run, sg_shfl<P>(a, kWarp - 1));
   }
   if (lane == 0) s_warp[warp] = run;
@@ -276,20 +304,31 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
     if (lane == 0) s_prefix = excl;
   }
   __syncthreads();
-  // Inclusive output: the running value after each element.  Exclusive
-  // output: init for a segment's first element, else init op the running
-  // value before it.
+  // Pass 2: inclusive output is the running value after each element;
+  // exclusive output is init for a segment's first element, else init op the
+  // running value before it.
   const S pre = sg_comb<P>(s_prefix, warp_excl);
 #pragma unroll
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
-    S acc = sg_comb<P>(sg_comb<P>(pre, chunk_pre[j]), lane_excl[j]);
+    const uint32_t local = warp_first + j * (kWarp * N) + lane * N;
+    const uint32_t hb = (s_heads[local >> 5] >> (local & 31u)) & ((1u << N) - 1u);
+    T x[N];
+    if (vec_in && e0 + N <= n) {
+      const SegVec<T, N> w = *reinterpret_cast<const SegVec<T, N> *>(in + e0);
+#pragma unroll
+      for (int m = 0; m < N; ++m) x[m] = w.v[m];
+    } else {
+#pragma unroll
+      for (int m = 0; m < N; ++m) x[m] = (e0 + m < n) ? in[e0 + m] : T(0);
+    }
+    S acc = sg_comb<P>(pre, lane_pre[j]);
     T y[N];
 #pragma unroll
     for (int m = 0; m < N; ++m) {
-      const uint32_t h = (hb[j] >> m) & 1u;
+      const uint32_t h = (hb >> m) & 1u;
       const Acc ex = h ? init : P::comb(init, acc.v);
-      acc = sg_comb<P>(acc, S{h, (e0 + m < n) ? P::from(x[j][m]) : P::ident()});
+      acc = sg_comb<P>(acc, S{h, (e0 + m < n) ? P::from(x[m]) : P::ident()});
       y[m] = P::out(exclusive ? ex : acc.v);
     }
     if (vec_out && e0 + N <= n) {
@@ -342,11 +381,11 @@ segmented_reduce_kernel(const T *__restrict__ in, const unsigned long long *__re
   }
 }
 
-// Tile shapes the segmented scan is compiled for: 8 or 16 items per thread
-// for 4-byte elements, 4 or 8 for wider ones (tunable "items_per_thread").
+// Tile shapes the segmented scan is compiled for: 16 or 32 items per thread
+// for 4-byte elements, 8 or 16 for wider ones (tunable "items_per_thread").
 template <class T> struct SegScanShapes {
-  static constexpr int small = sizeof(T) == 4 ? 8 : 4;
-  static constexpr int large = sizeof(T) == 4 ? 16 : 8;
+  static constexpr int small = sizeof(T) == 4 ? 16 : 8;
+  static constexpr int large = sizeof(T) == 4 ? 32 : 16;
 };
 
 std::string seg_object(const char *what, bcx_dtype t) { return std::string(what) + "_" + dtype_name(t); }
@@ -354,15 +393,23 @@ std::string seg_object(const char *what, bcx_dtype t) { return std::string(what)
 template <class T, class P, int ITEMS>
 bcx_status launch_segmented_scan(cudaStream_t s, int exclusive, const T &init_v, const void *in, void *out,
                                  size_t n, const unsigned long long *offsets, size_t nseg, char *base,
-                                 const SgStatus<P> &st, DeviceState *ds) {
-  const size_t tiles = div_up(n, size_t(kSegThreads) * ITEMS);
+                                 uint32_t *tile_first_seg, const SgStatus<P> &st, DeviceState *ds) {
+  const size_t tile = size_t(kSegThreads) * ITEMS;
+  const size_t tiles = div_up(n, tile);
+  {
+    KernelScope ks("segmented_scan_plan", s);
+    seg_tile_first_kernel<<<unsigned(div_up(tiles, size_t(256))), 256, 0, s>>>(offsets, nseg, tile, tiles,
+                                                                               tile_first_seg);
+    const bcx_status rc = launch_status("segmented_scan_plan");
+    if (rc) return rc;
+  }
   constexpr int N = 16 / int(sizeof(T)) < ITEMS ? 16 / int(sizeof(T)) : ITEMS;
   const int vec_in = reinterpret_cast<uintptr_t>(in) % (sizeof(T) * N) == 0;
   const int vec_out = reinterpret_cast<uintptr_t>(out) % (sizeof(T) * N) == 0;
   KernelScope ks("segmented_scan", s);
   segmented_scan_kernel<T, P, ITEMS><<<unsigned(tiles), kSegThreads, 0, s>>>(
-      static_cast<const T *>(in), static_cast<T *>(out), n, offsets, nseg, exclusive, P::from_host(init_v), st,
-      reinterpret_cast<uint32_t *>(base), vec_in, vec_out, ds->err_word);
+      static_cast<const T *>(in), static_cast<T *>(out), n, offsets, nseg, tile_first_seg, exclusive,
+      P::from_host(init_v), st, reinterpret_cast<uint32_t *>(base), vec_in, vec_out, ds->err_word);
   return launch_status("segmented_scan");
 }
 
@@ -370,31 +417,34 @@ template <class T, class P>
 bcx_status run_segmented_scan(cudaStream_t s, bcx_dtype type, int exclusive, const void *init, const void *in,
                               void *out, size_t n, const unsigned long long *offsets, size_t nseg, void *temp,
                               size_t *temp_bytes) {
-  typedef Sg<P> S;
   typedef SegScanShapes<T> Shapes;
+  typedef SgStatus<P> Status;
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;
+  BCX_CHECK(nseg < (size_t(1) << 32), BCX_INVALID_VALUE, "segmented scan: too many segments");
   // Storage for the most tiles any compiled shape makes, so the size does not
-  // depend on the tuned shape.
+  // depend on the tuned shape.  Layout: ticket line | status | tile -> first
+  // segment.
   const size_t tiles = div_up(n, size_t(kSegThreads) * Shapes::small);
-  const size_t need = 256 + align256(tiles * 4) + 2 * align256(tiles * sizeof(S));
+  const size_t need = 256 + Status::bytes(tiles) + align256(tiles * 4);
   TempStorage ts;
   bool query = false;
   rc = ts.acquire(temp, temp_bytes, need, s, &query);
   if (rc || query) return rc;
   char *base = static_cast<char *>(ts.ptr());
-  SgStatus<P> st;
-  st.flags = reinterpret_cast<uint32_t *>(base + 256);
-  st.agg = reinterpret_cast<S *>(base + 256 + align256(tiles * 4));
-  st.inc = reinterpret_cast<S *>(base + 256 + align256(tiles * 4) + align256(tiles * sizeof(S)));
-  BCX_CUDA(cudaMemsetAsync(base, 0, 256 + align256(tiles * 4), s));
+  Status st;
+  st.bind(base + 256, tiles);
+  uint32_t *tile_first_seg = reinterpret_cast<uint32_t *>(base + 256 + Status::bytes(tiles));
+  BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
   T init_v;
   memcpy(&init_v, init, sizeof(T));
   const uint32_t items = param_get(seg_object("segmented_scan", type), "items_per_thread", uint32_t(Shapes::small));
   if (items == uint32_t(Shapes::large))
-    return launch_segmented_scan<T, P, Shapes::large>(s, exclusive, init_v, in, out, n, offsets, nseg, base, st, ds);
-  return launch_segmented_scan<T, P, Shapes::small>(s, exclusive, init_v, in, out, n, offsets, nseg, base, st, ds);
+    return launch_segmented_scan<T, P, Shapes::large>(s, exclusive, init_v, in, out, n, offsets, nseg, base,
+                                                      tile_first_seg, st, ds);
+  return launch_segmented_scan<T, P, Shapes::small>(s, exclusive, init_v, in, out, n, offsets, nseg, base,
+                                                    tile_first_seg, st, ds);
 }
 
 template <class T, class P>
