@@ -156,6 +156,7 @@ struct TileStatus<Carry, true> {
   static size_t bytes(size_t tiles) { return align256(tiles * 8); }
   static size_t zero_bytes(size_t tiles) { return bytes(tiles); }
   void bind(char *base, size_t) { words = reinterpret_cast<unsigned long long *>(base); }
+  cudaError_t clear(size_t tiles, cudaStream_t s) const { return cudaMemsetAsync(words, 0, zero_bytes(tiles), s); }
   __device__ __forceinline__ void publish(size_t t, uint32_t flag, Carry v) {
     uint32_t bits;
     memcpy(&bits, &v, 4);
@@ -185,6 +186,7 @@ struct TileStatus<Carry, false> {
     agg = reinterpret_cast<Carry *>(base + align256(tiles * 4));
     inc = reinterpret_cast<Carry *>(base + align256(tiles * 4) + align256(tiles * sizeof(Carry)));
   }
+  cudaError_t clear(size_t tiles, cudaStream_t s) const { return cudaMemsetAsync(flags, 0, zero_bytes(tiles), s); }
   __device__ __forceinline__ void publish(size_t t, uint32_t flag, Carry v) {
     if (flag == kFlagAggregate) agg[t] = v;
     else inc[t] = v;
@@ -195,6 +197,44 @@ struct TileStatus<Carry, false> {
     if (f == kFlagAggregate) *v = ldcg(&agg[t]);
     else if (f == kFlagPrefix) *v = ldcg(&inc[t]);
     return f;
+  }
+};
+
+// FP64 carries (double scans, compensated float scans): the aggregate and the
+// inclusive prefix of a tile each live in one 64-bit word that holds either the
+// value or an all-ones bit pattern meaning "not published yet".  All ones is a
+// NaN with a full payload, which GPU arithmetic never produces (computed NaNs
+// are canonical), and a relaxed 64-bit load returns either the marker or the
+// whole value, so no fence has to order a separate flag after the value.
+template <>
+struct TileStatus<double, false> {
+  unsigned long long *agg;
+  unsigned long long *inc;
+  static constexpr unsigned long long kUnset = ~0ull;
+  static size_t bytes(size_t tiles) { return 2 * align256(tiles * 8); }
+  void bind(char *base, size_t tiles) {
+    agg = reinterpret_cast<unsigned long long *>(base);
+    inc = reinterpret_cast<unsigned long long *>(base + align256(tiles * 8));
+  }
+  cudaError_t clear(size_t tiles, cudaStream_t s) const { return cudaMemsetAsync(agg, 0xff, bytes(tiles), s); }
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, double v) {
+    unsigned long long w;
+    memcpy(&w, &v, 8);
+    unsigned long long *dst = flag == kFlagAggregate ? &agg[t] : &inc[t];
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(dst), "l"(w) : "memory");
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, double *v) const {
+    const unsigned long long wi = ld_relaxed_u64(&inc[t]);
+    const unsigned long long wa = ld_relaxed_u64(&agg[t]);
+    if (wi != kUnset) {
+      memcpy(v, &wi, 8);
+      return kFlagPrefix;
+    }
+    if (wa != kUnset) {
+      memcpy(v, &wa, 8);
+      return kFlagAggregate;
+    }
+    return kFlagInvalid;
   }
 };
 
@@ -465,7 +505,8 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   uint32_t *counter = reinterpret_cast<uint32_t *>(base);
   Status st;
   st.bind(base + 256, tiles);
-  BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
+  BCX_CUDA(cudaMemsetAsync(base, 0, 256, s));
+  BCX_CUDA(st.clear(tiles, s));
   BCX_CHECK(tiles < (size_t(1) << 31), BCX_INVALID_VALUE, "scan: input too large");
   KernelScope ks("scan_lookback", s);
   scan_tile_kernel<T, P, kScanThreads, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
@@ -637,7 +678,8 @@ bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, c
   Status st;
   st.bind(base + 256, tiles);
   // The array keeps the previous call's tickets and flags: clear them.
-  BCX_CUDA(cudaMemsetAsync(base, 0, 256 + Status::zero_bytes(tiles), s));
+  BCX_CUDA(cudaMemsetAsync(base, 0, 256, s));
+  BCX_CUDA(st.clear(tiles, s));
   KernelScope ks("scan_lookback", s);
   scan_tile_kernel<T, P, kNoAllocThreads, V, false, Status><<<unsigned(tiles), kNoAllocThreads, 0, s>>>(
       pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);
