@@ -8,6 +8,8 @@
 #include <boost/compute/algorithm/inner_product.hpp>
 #include <boost/compute/algorithm/max_element.hpp>
 #include <boost/compute/algorithm/min_element.hpp>
+#include <boost/compute/algorithm/partition.hpp>
+#include <boost/compute/algorithm/unique.hpp>
 #include <boost/compute/algorithm/reduce.hpp>
 #include <boost/compute/algorithm/reduce_by_key.hpp>
 #include <boost/compute/algorithm/scan.hpp>

@@ -33,6 +33,29 @@ inline size_t mark_and_scan(const A *in, size_t n, const std::string &defs, cons
   return size_t(last_pos) + size_t(last_mark);
 }
 
+// marks[i] = EXPR ? 1 : 0 where _1 = in[i], _0 = in[i - 1] (in[i] for i == 0)
+// and first = (i == 0): predicates that look at the previous element.
+template <class A>
+inline size_t mark_adjacent_and_scan(const A *in, size_t n, const std::string &defs, const std::string &expr,
+                                     vector<uint_> &marks, vector<uint_> &pos, command_queue &queue) {
+  std::ostringstream src;
+  src << jit_prelude() << defs << "\nextern \"C\" __global__ void bcx_jit_mark_adjacent(const "
+      << cuda_type_name<A>::get() << " *__restrict__ in, unsigned *__restrict__ marks, unsigned long long n) {\n"
+      << "  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;"
+      << " i += (unsigned long long)gridDim.x * blockDim.x) {\n"
+      << "    const auto _1 = in[i];\n    const auto _0 = in[i > 0 ? i - 1 : 0];\n    const bool first = i == 0;\n"
+      << "    marks[i] = (" << expr << ") ? 1u : 0u;\n  }\n}\n";
+  unsigned *m = marks.data();
+  unsigned long long nn = n;
+  void *args[] = {(void *)&in, (void *)&m, (void *)&nn};
+  jit_launch(src.str(), "bcx_jit_mark_adjacent", grid_for(n, 256), 256, queue, args);
+  const uint_ zero = 0;
+  check(bcx_scan(queue.get(), BCX_UINT, BCX_PLUS, 1, &zero, marks.data(), pos.data(), n, 0, nullptr, nullptr));
+  const uint_ last_pos = (pos.begin() + std::ptrdiff_t(n - 1)).read(queue);
+  const uint_ last_mark = (marks.begin() + std::ptrdiff_t(n - 1)).read(queue);
+  return size_t(last_pos) + size_t(last_mark);
+}
+
 template <class A, class T>
 inline void scatter_marked(const A *in, const vector<uint_> &marks, const vector<uint_> &pos, size_t n, T *out,
                            command_queue &queue) {

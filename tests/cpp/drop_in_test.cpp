@@ -344,6 +344,51 @@ static void scan_family_cases(compute::command_queue &q) {
   CHECK(all2);
 }
 
+static void compaction_cases(compute::command_queue &q) {
+  using compute::_1;
+  using compute::_2;
+  // test/test_unique.cpp
+  int ud[] = {1, 1, 2, 2, 2, 3, 1, 1, 5};
+  compute::vector<int> uv(ud, ud + 9, q);
+  auto uend = compute::unique(uv.begin(), uv.end(), q);
+  std::vector<int> hu = to_host(uv, q);
+  CHECK(uend - uv.begin() == 5 && (std::vector<int>(hu.begin(), hu.begin() + 5) == std::vector<int>{1, 2, 3, 1, 5}));
+  // unique_copy with a custom predicate: runs of elements within 1 of their predecessor
+  int cd[] = {10, 11, 12, 20, 21, 30, 31, 32, 33};
+  compute::vector<int> cv(cd, cd + 9, q), co(9, q.get_context());
+  BOOST_COMPUTE_FUNCTION(bool, close_to, (int a, int b), { return b - a == 1; });
+  auto cend = compute::unique_copy(cv.begin(), cv.end(), co.begin(), close_to, q);
+  std::vector<int> hc = to_host(co, q);
+  CHECK(cend - co.begin() == 3 && (std::vector<int>(hc.begin(), hc.begin() + 3) == std::vector<int>{10, 20, 30}));
+  // stable_partition keeps both halves in input order (test/test_stable_partition.cpp)
+  int pd[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10};
+  compute::vector<int> pv(pd, pd + 10, q);
+  auto mid = compute::stable_partition(pv.begin(), pv.end(), _1 % 2 == 0, q);
+  CHECK(mid - pv.begin() == 5);
+  CHECK((to_host(pv, q) == std::vector<int>{2, 4, 6, 8, 10, 1, 3, 5, 7, 9}));
+  // remove_if / remove (test/test_remove.cpp)
+  int rd[] = {1, 5, 2, 5, 3, 5, 4};
+  compute::vector<int> rv(rd, rd + 7, q);
+  auto rend = compute::remove(rv.begin(), rv.end(), 5, q);
+  std::vector<int> hr = to_host(rv, q);
+  CHECK(rend - rv.begin() == 4 && (std::vector<int>(hr.begin(), hr.begin() + 4) == std::vector<int>{1, 2, 3, 4}));
+  compute::vector<int> rv2(rd, rd + 7, q);
+  auto rend2 = compute::remove_if(rv2.begin(), rv2.end(), _1 < 3, q);
+  std::vector<int> hr2 = to_host(rv2, q);
+  CHECK(rend2 - rv2.begin() == 5 && (std::vector<int>(hr2.begin(), hr2.begin() + 5) == std::vector<int>{5, 5, 3, 5, 4}));
+  // a large unique: 2^20 + 9 elements in runs of 3
+  const size_t n = (1 << 20) + 9;
+  std::vector<int> big(n);
+  for (size_t i = 0; i < n; ++i) big[i] = int(i / 3);
+  compute::vector<int> bv(big.begin(), big.end(), q);
+  auto bend = compute::unique(bv.begin(), bv.end(), q);
+  CHECK(size_t(bend - bv.begin()) == (n + 2) / 3);
+  std::vector<int> hb = to_host(bv, q);
+  bool ok = true;
+  for (size_t i = 0; i < (n + 2) / 3; ++i) ok = ok && hb[i] == int(i);
+  CHECK(ok);
+}
+
 static void comparator_sort_cases(compute::command_queue &q) {
   using compute::_1;
   using compute::_2;
@@ -406,6 +451,7 @@ int main() {
   transform_reduce_cases(q);
   scan_family_cases(q);
   comparator_sort_cases(q);
+  compaction_cases(q);
   error_cases(q);
   q.check_device_errors();
   std::printf("%s (%d failures)\n", g_failures ? "FAILED" : "OK", g_failures);
