@@ -343,7 +343,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "uint32",
-                "data": "synthetic (seeded uniform 32-bit keys, iota values; BASELINE configs' shapes)",
+                "data": "synthetic (seeded uniform 32-bit keys, iota values; the configuration's shapes)",
                 "config": {"workload": WORKLOAD if N_SORT == 1 << 28 else f"sort_by_key uint32 pairs n={N_SORT}",
                            "l2": "inputs larger than L2: every step sorts its own buffer",
                            "parallelism": "replicas" if world > 1 else "single GPU"},

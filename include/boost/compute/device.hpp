@@ -1,6 +1,6 @@
 // boost/compute/device.hpp -- a CUDA device seen through the reference's
 // device interface (device.hpp: name(), compute_units(), type(),
-// global_memory_size()).  Every device of this build is a GPU.
+// global_memory_size()).  Every device this library drives is a CUDA GPU.
 #ifndef BOOST_COMPUTE_DEVICE_HPP
 #define BOOST_COMPUTE_DEVICE_HPP
 

@@ -4,7 +4,7 @@ Reads the Boost.Compute test sources (``test/test_*.cpp`` under the reference
 checkout given by ``--reference``) as text, pulls the literal input arrays and
 the literal expected values out of each listed test case, and writes
 ``reference_vectors.json`` next to this script.  Nothing is executed: the
-reference needs OpenCL and Boost, which this build does not have, so its own
+reference needs OpenCL and Boost, neither of which is installed here, so its own
 known-answer tests are the pin for the oracle and the CUDA path.
 
 Every case records its source file and line range so it can be checked
