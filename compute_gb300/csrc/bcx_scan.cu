@@ -461,11 +461,18 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   }
 }
 
-// 16-byte vectors per thread: 64 elements per thread when the accumulator is
-// at most 4 bytes (64 KB tiles of 4-byte elements), 32 compensated FP32
-// pairs, 8 elements of 8-byte types; larger shapes spill registers.
+// Tile shape of the allocating scan (measured on GB300 at 2^30 elements):
+// 96 elements per thread when the accumulator is at most 4 bytes (96 KB tiles
+// of 4-byte elements; 64 and 128 per thread were slower), 32 compensated FP32
+// pairs per thread in 512-thread blocks, 8 elements of 8-byte types.
 template <class T, class P> struct scan_vectors_per_thread {
-  static constexpr int value = sizeof(typename P::Acc) <= 4 ? int(64 / (16 / sizeof(T))) : (sizeof(T) == 4 ? 8 : 4);
+  static constexpr int value = sizeof(typename P::Acc) <= 4 ? int(96 / (16 / sizeof(T))) : (sizeof(T) == 4 ? 8 : 4);
+};
+template <class P> struct scan_threads {
+  static constexpr int value = kScanThreads;
+};
+template <> struct scan_threads<ScanCompF32> {
+  static constexpr int value = 512;
 };
 
 template <class T, class P>
@@ -475,6 +482,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   typedef TileStatus<Carry> Status;
   constexpr int N = 16 / sizeof(T);
   constexpr int V = scan_vectors_per_thread<T, P>::value;
+  constexpr int THREADS = scan_threads<P>::value;
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;
@@ -483,7 +491,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   const bool vec_ok = elem_aligned && ((ain & 15u) == (aout & 15u));
   const size_t head_pad = vec_ok ? (ain & 15u) / sizeof(T) : 0;
   const size_t nv = n + head_pad;
-  const size_t tile_elems = size_t(kScanThreads) * V * N;
+  const size_t tile_elems = size_t(THREADS) * V * N;
   const size_t tiles = div_up(nv, tile_elems);
   const bool single = (tiles <= 1);
   const size_t need = single ? 0 : (256 + Status::bytes(tiles));
@@ -497,7 +505,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   if (single) {
     Status st{};
     KernelScope ks("scan_single", s);
-    scan_tile_kernel<T, P, kScanThreads, V, true, Status><<<1, kScanThreads, 0, s>>>(
+    scan_tile_kernel<T, P, THREADS, V, true, Status><<<1, THREADS, 0, s>>>(
         pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, nullptr, ds->err_word);
     return launch_status("scan_single");
   }
@@ -509,7 +517,7 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   BCX_CUDA(st.clear(tiles, s));
   BCX_CHECK(tiles < (size_t(1) << 31), BCX_INVALID_VALUE, "scan: input too large");
   KernelScope ks("scan_lookback", s);
-  scan_tile_kernel<T, P, kScanThreads, V, false, Status><<<unsigned(tiles), kScanThreads, 0, s>>>(
+  scan_tile_kernel<T, P, THREADS, V, false, Status><<<unsigned(tiles), THREADS, 0, s>>>(
       pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);
   return launch_status("scan_lookback");
 }
