@@ -83,9 +83,6 @@ static_assert(sizeof(SortControl) == 256, "control block is 256 bytes");
 // only then rank keys stably and scatter them.
 constexpr int kLookbackWindow = 4;
 
-__device__ __forceinline__ void st_relaxed_u32(uint32_t *p, uint32_t v) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 // Exclusive prefix of digit `d` over the tiles first_tile .. tile-1 (the
 // tiles of the same sort, or of the same segment).  first_tile publishes its

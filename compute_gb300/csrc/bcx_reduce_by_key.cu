@@ -21,6 +21,8 @@
 // carries Neumaier (s, c) pairs.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "bcx.h"
 #include "bcx_common.cuh"
 #include "bcx_internal.h"
@@ -96,11 +98,41 @@ __device__ __forceinline__ void seg_push(Seg<P> &a, bool head, V x) {
   }
 }
 
+// Look-back status of one tile, published twice (aggregate, then inclusive
+// prefix).  Every word starts as all ones ("unset") and is written once, so a
+// relaxed load sees either "unset" or the final value and no fence is needed:
+//   kind 1 (4-byte values): run count word and value share one 64-bit word;
+//          a count of all ones cannot occur below 2^31 - 1 elements;
+//   kind 2 (double, and compensated float carried as the FP64 sum of its
+//          pair): a count word plus a 64-bit value word whose all-ones pattern
+//          is a NaN GPU arithmetic never produces (computed NaNs are
+//          canonical); a poll is ready when both are set;
+//   kind 0 (8-byte integers, where every bit pattern is a value): a flag word
+//          plus aggregate/inclusive arrays ordered by release/acquire.
 template <class P>
-struct RbStatus {
+struct RbStatusKind {
+  typedef typename P::Acc Acc;
+  static constexpr int value = sizeof(Acc) == 4                          ? 1
+                               : std::is_same<Acc, double>::value        ? 2
+                               : std::is_same<Acc, comp_f32>::value      ? 2
+                                                                         : 0;
+};
+
+template <class P, int KIND = RbStatusKind<P>::value>
+struct RbStatus;
+
+template <class P>
+struct RbStatus<P, 0> {
   uint32_t *flags;
   Seg<P> *agg;
   Seg<P> *inc;
+  static size_t bytes(size_t tiles) { return align256(tiles * 4) + 2 * align256(tiles * sizeof(Seg<P>)); }
+  void bind(char *base, size_t tiles) {
+    flags = reinterpret_cast<uint32_t *>(base);
+    agg = reinterpret_cast<Seg<P> *>(base + align256(tiles * 4));
+    inc = reinterpret_cast<Seg<P> *>(base + align256(tiles * 4) + align256(tiles * sizeof(Seg<P>)));
+  }
+  cudaError_t clear(size_t tiles, cudaStream_t s) const { return cudaMemsetAsync(flags, 0, align256(tiles * 4), s); }
   __device__ __forceinline__ void publish(size_t t, uint32_t flag, const Seg<P> &s) {
     if (flag == kRbAggregate) agg[t] = s;
     else inc[t] = s;
@@ -117,6 +149,90 @@ struct RbStatus {
       memcpy(s, tmp, sizeof(Seg<P>));
     }
     return f;
+  }
+};
+
+template <class P>
+struct RbStatus<P, 1> {
+  unsigned long long *agg;
+  unsigned long long *inc;
+  static size_t bytes(size_t tiles) { return 2 * align256(tiles * 8); }
+  void bind(char *base, size_t tiles) {
+    agg = reinterpret_cast<unsigned long long *>(base);
+    inc = reinterpret_cast<unsigned long long *>(base + align256(tiles * 8));
+  }
+  cudaError_t clear(size_t tiles, cudaStream_t s) const { return cudaMemsetAsync(agg, 0xff, bytes(tiles), s); }
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, const Seg<P> &s) {
+    uint32_t vb;
+    memcpy(&vb, &s.v, 4);
+    const unsigned long long w = (static_cast<unsigned long long>(vb) << 32) | s.c;
+    unsigned long long *dst = flag == kRbAggregate ? &agg[t] : &inc[t];
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(dst), "l"(w) : "memory");
+  }
+  __device__ __forceinline__ static bool unpack(unsigned long long w, Seg<P> *s) {
+    if (uint32_t(w) == 0xffffffffu) return false;
+    s->c = uint32_t(w);
+    const uint32_t vb = uint32_t(w >> 32);
+    memcpy(&s->v, &vb, 4);
+    return true;
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, Seg<P> *s) const {
+    const unsigned long long wi = ld_relaxed_u64(&inc[t]);
+    const unsigned long long wa = ld_relaxed_u64(&agg[t]);
+    if (unpack(wi, s)) return kRbPrefix;
+    if (unpack(wa, s)) return kRbAggregate;
+    return kRbInvalid;
+  }
+};
+
+// FP64 view of a value (the compensated pair as its exact-in-double sum).
+__device__ __forceinline__ double rb_to_f64(double v) { return v; }
+__device__ __forceinline__ double rb_to_f64(comp_f32 v) { return double(v.s) + double(v.c); }
+__device__ __forceinline__ void rb_from_f64(double d, double *v) { *v = d; }
+__device__ __forceinline__ void rb_from_f64(double d, comp_f32 *v) {
+  v->s = float(d);
+  v->c = float(d - double(v->s));
+}
+
+template <class P>
+struct RbStatus<P, 2> {
+  uint32_t *agg_c;
+  uint32_t *inc_c;
+  unsigned long long *agg_v;
+  unsigned long long *inc_v;
+  static size_t bytes(size_t tiles) { return 2 * align256(tiles * 4) + 2 * align256(tiles * 8); }
+  void bind(char *base, size_t tiles) {
+    agg_c = reinterpret_cast<uint32_t *>(base);
+    inc_c = reinterpret_cast<uint32_t *>(base + align256(tiles * 4));
+    agg_v = reinterpret_cast<unsigned long long *>(base + 2 * align256(tiles * 4));
+    inc_v = reinterpret_cast<unsigned long long *>(base + 2 * align256(tiles * 4) + align256(tiles * 8));
+  }
+  cudaError_t clear(size_t tiles, cudaStream_t s) const { return cudaMemsetAsync(agg_c, 0xff, bytes(tiles), s); }
+  __device__ __forceinline__ void publish(size_t t, uint32_t flag, const Seg<P> &s) {
+    const double d = rb_to_f64(s.v);
+    unsigned long long w;
+    memcpy(&w, &d, 8);
+    uint32_t *dc = flag == kRbAggregate ? &agg_c[t] : &inc_c[t];
+    unsigned long long *dv = flag == kRbAggregate ? &agg_v[t] : &inc_v[t];
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(dv), "l"(w) : "memory");
+    st_relaxed_u32(dc, s.c);
+  }
+  __device__ __forceinline__ static bool take(uint32_t c, unsigned long long w, Seg<P> *s) {
+    if (c == 0xffffffffu || w == ~0ull) return false;
+    double d;
+    memcpy(&d, &w, 8);
+    s->c = c;
+    rb_from_f64(d, &s->v);
+    return true;
+  }
+  __device__ __forceinline__ uint32_t poll(size_t t, Seg<P> *s) const {
+    const uint32_t ci = ld_relaxed_u32(&inc_c[t]);
+    const unsigned long long wi = ld_relaxed_u64(&inc_v[t]);
+    const uint32_t ca = ld_relaxed_u32(&agg_c[t]);
+    const unsigned long long wa = ld_relaxed_u64(&agg_v[t]);
+    if (take(ci, wi, s)) return kRbPrefix;
+    if (take(ca, wa, s)) return kRbAggregate;
+    return kRbInvalid;
   }
 };
 
@@ -323,20 +439,20 @@ bcx_status run_rbk(cudaStream_t s, const void *keys, const void *vals, size_t n,
   if (rc) return rc;
   const size_t tiles = div_up(n, size_t(Sh::TILE));
   const bool single = tiles <= 1;
-  const size_t need = single ? 0 : 256 + align256(tiles * 4) + 2 * align256(tiles * sizeof(S));
+  typedef RbStatus<P> Status;
+  const size_t need = single ? 0 : 256 + Status::bytes(tiles);
   TempStorage ts;
   bool query = false;
   rc = ts.acquire(temp, temp_bytes, need, s, &query);
   if (rc || query) return rc;
-  RbStatus<P> st{nullptr, nullptr, nullptr};
+  Status st{};
   uint32_t *counter = nullptr;
   if (!single) {
     char *base = static_cast<char *>(ts.ptr());
     counter = reinterpret_cast<uint32_t *>(base);
-    st.flags = reinterpret_cast<uint32_t *>(base + 256);
-    st.agg = reinterpret_cast<S *>(base + 256 + align256(tiles * 4));
-    st.inc = reinterpret_cast<S *>(base + 256 + align256(tiles * 4) + align256(tiles * sizeof(S)));
-    BCX_CUDA(cudaMemsetAsync(base, 0, 256 + align256(tiles * 4), s));
+    st.bind(base + 256, tiles);
+    BCX_CUDA(cudaMemsetAsync(base, 0, 256, s));
+    BCX_CUDA(st.clear(tiles, s));
   }
   const int vec_k = reinterpret_cast<uintptr_t>(keys) % (sizeof(K) * Sh::N) == 0;
   const int vec_v = reinterpret_cast<uintptr_t>(vals) % (sizeof(V) * Sh::N) == 0;
@@ -389,7 +505,7 @@ extern "C" bcx_status bcx_reduce_by_key(bcx_stream stream, bcx_dtype key_type, b
   using namespace bcx;
   clear_error();
   BCX_CHECK(dtype_valid(key_type) && dtype_valid(value_type), BCX_INVALID_VALUE, "invalid dtype");
-  BCX_CHECK(n < (size_t(1) << 31), BCX_INVALID_VALUE, "reduce_by_key: n must be below 2^31");
+  BCX_CHECK(n < (size_t(1) << 31) - 1, BCX_INVALID_VALUE, "reduce_by_key: n must be below 2^31 - 1");
   cudaStream_t s = (cudaStream_t)stream;
   if (n == 0) {
     if (temp == nullptr && temp_bytes != nullptr) {
