@@ -98,6 +98,8 @@ bcx_status param_save();
 // Largest small-segment tile the segmented sort is compiled for with these
 // key and value sizes (bcx_segmented_sort.cu).
 uint32_t segsort_small_tile_limit(size_t key_bytes, size_t value_bytes);
+// Items per thread the segmented scan is compiled for (bcx_segmented.cu).
+void segscan_shapes(size_t elem_bytes, uint32_t *small, uint32_t *large);
 
 // One piece of a batched gather/scatter: `bytes` bytes from src to dst, both
 // device-accessible.  The request server splits every buffer it moves into

@@ -175,7 +175,7 @@ struct alignas(sizeof(T) * N) SegVec {
 // consecutive elements chunk_base + l*N .. + N-1 (one vector load and store
 // when the arrays are aligned), so (j, l, m) is input order within a warp.
 template <class T, class P, int ITEMS>
-__global__ void __launch_bounds__(kSegThreads)
+__global__ void __launch_bounds__(kSegThreads, 4)
 segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
                       const unsigned long long *__restrict__ offsets, size_t nseg,
                       const uint32_t *__restrict__ tile_first_seg, int exclusive, typename P::Acc init,
@@ -198,25 +198,9 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
   const size_t tile_base = tile * TILE;
   const size_t tile_end = (tile_base + TILE < n) ? tile_base + TILE : n;
   const uint32_t warp_first = warp * (kWarp * ITEMS);
-  // Pass 1 over the tile: loads first (cached in L2 for the second read), so
-  // they are in flight while warp 0 marks the segment starts.
-  T x[CH][N];
-#pragma unroll
-  for (int j = 0; j < CH; ++j) {
-    const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
-    if (vec_in && e0 + N <= n) {
-      const uint4 u = __ldcg(reinterpret_cast<const uint4 *>(in + e0));
-      SegVec<T, N> w;
-      memcpy(&w, &u, sizeof(w));
-#pragma unroll
-      for (int m = 0; m < N; ++m) x[j][m] = w.v[m];
-    } else {
-#pragma unroll
-      for (int m = 0; m < N; ++m) x[j][m] = (e0 + m < n) ? in[e0 + m] : T(0);
-    }
-  }
   // Mark the segment starts inside this tile (offsets[0..nseg] are starts;
-  // offsets[nseg] == n is not).
+  // offsets[nseg] == n is not); the tile's first candidate segment comes from
+  // the pre-pass, so this is one load and usually a single iteration.
   if (warp == 0) {
     const size_t first = tile_first_seg[tile];
     for (size_t k = first + lane; k < nseg; k += kWarp) {
@@ -227,30 +211,50 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
     }
   }
   __syncthreads();  // head bitmap complete
-  // Per chunk: serial fold of the lane's run, warp scan of the lane folds.
-  // Only these prefixes stay in registers across the look-back; the tile is
-  // read again (from L2) for the outputs.
+  // Pass 1: per chunk, serial fold of the lane's run and a warp scan of the
+  // lane folds, G chunks loaded at a time (cached in L2 for the second read).
+  // Only the per-chunk prefixes stay in registers across the look-back.
+  constexpr int G = CH < 4 ? CH : 4;
   S lane_pre[CH];  // fold of everything before the lane's run in chunk j (within the warp)
   S run = sg_ident<P>();
 #pragma unroll
-  for (int j = 0; j < CH; ++j) {
-    const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
-    const uint32_t local = warp_first + j * (kWarp * N) + lane * N;
-    const uint32_t hb = (s_heads[local >> 5] >> (local & 31u)) & ((1u << N) - 1u);
-    S a = sg_ident<P>();
+  for (int g = 0; g < CH; g += G) {
+    T x[G][N];
 #pragma unroll
-    for (int m = 0; m < N; ++m) {
-      const S e{(hb >> m) & 1u, (e0 + m < n) ? P::from(x[j][m]) : P::ident()};
-      a = sg_comb<P>(a, e);
+    for (int c = 0; c < G; ++c) {
+      const size_t e0 = tile_base + warp_first + (g + c) * (kWarp * N) + lane * N;
+      if (vec_in && e0 + N <= n) {
+        const uint4 u = __ldcg(reinterpret_cast<const uint4 *>(in + e0));
+        SegVec<T, N> w;
+        memcpy(&w, &u, sizeof(w));
+#pragma unroll
+        for (int m = 0; m < N; ++m) x[c][m] = w.v[m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < N; ++m) x[c][m] = (e0 + m < n) ? in[e0 + m] : T(0);
+      }
     }
 #pragma unroll
-    for (int d = 1; d < kWarp; d <<= 1) {
-      const S o = sg_shfl_up<P>(a, d);
-      if (int(lane) >= d) a = sg_comb<P>(o, a);
+    for (int c = 0; c < G; ++c) {
+      const int j = g + c;
+      const size_t e0 = tile_base + warp_first + j * (kWarp * N) + lane * N;
+      const uint32_t local = warp_first + j * (kWarp * N) + lane * N;
+      const uint32_t hb = (s_heads[local >> 5] >> (local & 31u)) & ((1u << N) - 1u);
+      S a = sg_ident<P>();
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        const S e{(hb >> m) & 1u, (e0 + m < n) ? P::from(x[c][m]) : P::ident()};
+        a = sg_comb<P>(a, e);
+      }
+#pragma unroll
+      for (int d = 1; d < kWarp; d <<= 1) {
+        const S o = sg_shfl_up<P>(a, d);
+        if (int(lane) >= d) a = sg_comb<P>(o, a);
+      }
+      const S ex = sg_shfl_up<P>(a, 1);
+      lane_pre[j] = lane == 0 ? run : sg_comb<P>(run, ex);
+      run = sg_comb<P>(run, sg_shfl<P>(a, kWarp - 1));
     }
-    const S ex = sg_shfl_up<P>(a, 1);
-    lane_pre[j] = lane == 0 ? run : sg_comb<P>(run, ex);
-    run = sg_comb<P>(run, sg_shfl<P>(a, kWarp - 1));
   }
   if (lane == 0) s_warp[warp] = run;
   __syncthreads();
@@ -381,11 +385,11 @@ segmented_reduce_kernel(const T *__restrict__ in, const unsigned long long *__re
   }
 }
 
-// Tile shapes the segmented scan is compiled for: 16 or 32 items per thread
+// Tile shapes the segmented scan is compiled for: 32 or 64 items per thread
 // for 4-byte elements, 8 or 16 for wider ones (tunable "items_per_thread").
 template <class T> struct SegScanShapes {
-  static constexpr int small = sizeof(T) == 4 ? 16 : 8;
-  static constexpr int large = sizeof(T) == 4 ? 32 : 16;
+  static constexpr int small = sizeof(T) == 4 ? 32 : 8;
+  static constexpr int large = sizeof(T) == 4 ? 64 : 16;
 };
 
 std::string seg_object(const char *what, bcx_dtype t) { return std::string(what) + "_" + dtype_name(t); }
@@ -510,6 +514,17 @@ bcx_status seg_dispatch(bcx_dtype t, int op, int comp, Fn &&fn) {
 }
 
 }  // namespace
+
+void segscan_shapes(size_t elem_bytes, uint32_t *small, uint32_t *large) {
+  if (elem_bytes == 4) {
+    *small = SegScanShapes<int32_t>::small;
+    *large = SegScanShapes<int32_t>::large;
+  } else {
+    *small = SegScanShapes<int64_t>::small;
+    *large = SegScanShapes<int64_t>::large;
+  }
+}
+
 }  // namespace bcx
 
 using namespace bcx;

@@ -356,7 +356,9 @@ bcx_status bcx_tune_segmented_scan(bcx_stream stream, bcx_dtype type, const void
     return bcx_segmented_scan(stream, type, BCX_PLUS, 1, zero, in, out, n, offsets, nseg, comp, tmp, &t);
   };
   const std::string obj = std::string("segmented_scan_") + dtype_name(type);
-  const std::vector<uint32_t> items = es == 4 ? std::vector<uint32_t>{8u, 16u} : std::vector<uint32_t>{4u, 8u};
+  uint32_t small = 0, large = 0;
+  segscan_shapes(es, &small, &large);
+  const std::vector<uint32_t> items{small, large};
   if ((rc = tune_param(s, obj, "items_per_thread", items, rep, reset, run))) return rc;
   return param_save();
 }

@@ -332,7 +332,7 @@ bcx_status bcx_device_sm_count(int *sm_count);
  *   "segmented_sort_k<key bits>_v<value bytes>": "small_tile" (1024, 2048 or
  *       4096: segments up to this many pairs sort in shared memory),
  *       "small_blocks_per_sm" (0 = as many as fit);
- *   "segmented_scan_<type>": "items_per_thread" (8/16 for 4-byte types, 4/8
+ *   "segmented_scan_<type>": "items_per_thread" (32/64 for 4-byte types, 8/16
  *       for 8-byte types);
  *   "segmented_reduce_<type>": "blocks_per_sm".
  * Temporary-storage sizes never depend on these values. */

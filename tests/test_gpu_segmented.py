@@ -180,7 +180,7 @@ def test_segmented_sort_every_small_tile(cuda, tile, per_sm):
         np.testing.assert_array_equal(gv[a:b], rv, err_msg=f"values seg {s}")
 
 
-@pytest.mark.parametrize("dtype,items", [("int", 16), ("int", 8), ("long", 4), ("float", 16)])
+@pytest.mark.parametrize("dtype,items", [("int", 32), ("int", 64), ("long", 8), ("long", 16), ("float", 64)])
 def test_segmented_scan_every_tile(cuda, dtype, items):
     rng = np.random.default_rng(items)
     offsets = log_uniform_offsets(rng, 500, 1, 30_000, empty_frac=0.05)
