@@ -406,7 +406,7 @@ def run_e2e(torch, bc, rank, world):
     hv = torch.arange(N_SORT, dtype=torch.int32).pin_memory()
     src_k = torch.from_numpy(hk0.view(np.int32))
     src_v = torch.arange(N_SORT, dtype=torch.int32)
-    e2e_steps = 8
+    e2e_steps = 16
     for _ in range(3):  # warm-up (pool, page-locked pages, copy engines)
         bc.sort_by_key_host(hk, hv, dtype="uint")
     tot = 0.0
