@@ -166,6 +166,10 @@ __global__ void seg_tile_first_kernel(const unsigned long long *__restrict__ off
   tile_first_seg[t] = uint32_t(lo);
 }
 
+// Bytes of consecutive elements a lane owns per chunk of the segmented scan
+// (a multiple of 16: one or more 16-byte vector loads).
+constexpr int kSegRunBytes = 16;
+
 template <class T, int N>
 struct alignas(sizeof(T) * N) SegVec {
   T v[N];
@@ -182,7 +186,7 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
                       SgStatus<P> st, uint32_t *__restrict__ tile_counter, int vec_in, int vec_out, uint32_t *err) {
   typedef Sg<P> S;
   typedef typename P::Acc Acc;
-  constexpr int N = 16 / int(sizeof(T)) < ITEMS ? 16 / int(sizeof(T)) : ITEMS;
+  constexpr int N = kSegRunBytes / int(sizeof(T)) < ITEMS ? kSegRunBytes / int(sizeof(T)) : ITEMS;
   constexpr int CH = ITEMS / N;
   constexpr int TILE = kSegThreads * ITEMS;
   static_assert(32 % N == 0, "a lane's run sits inside one bitmap word");
@@ -224,9 +228,11 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
     for (int c = 0; c < G; ++c) {
       const size_t e0 = tile_base + warp_first + (g + c) * (kWarp * N) + lane * N;
       if (vec_in && e0 + N <= n) {
-        const uint4 u = __ldcg(reinterpret_cast<const uint4 *>(in + e0));
         SegVec<T, N> w;
-        memcpy(&w, &u, sizeof(w));
+        uint4 u[sizeof(w) / 16];
+#pragma unroll
+        for (int q = 0; q < int(sizeof(w) / 16); ++q) u[q] = __ldcg(reinterpret_cast<const uint4 *>(in + e0) + q);
+        memcpy(&w, u, sizeof(w));
 #pragma unroll
         for (int m = 0; m < N; ++m) x[c][m] = w.v[m];
       } else {
@@ -407,7 +413,7 @@ bcx_status launch_segmented_scan(cudaStream_t s, int exclusive, const T &init_v,
     const bcx_status rc = launch_status("segmented_scan_plan");
     if (rc) return rc;
   }
-  constexpr int N = 16 / int(sizeof(T)) < ITEMS ? 16 / int(sizeof(T)) : ITEMS;
+  constexpr int N = kSegRunBytes / int(sizeof(T)) < ITEMS ? kSegRunBytes / int(sizeof(T)) : ITEMS;
   const int vec_in = reinterpret_cast<uintptr_t>(in) % (sizeof(T) * N) == 0;
   const int vec_out = reinterpret_cast<uintptr_t>(out) % (sizeof(T) * N) == 0;
   KernelScope ks("segmented_scan", s);
