@@ -44,6 +44,9 @@ namespace {
 // Block size of the allocating scan (the no-alloc entry point keeps its own
 // fixed shape).
 constexpr int kScanThreads = 256;
+// 16-byte vectors a lane owns consecutively per chunk (its serial run before
+// the chunk's warp scan).
+constexpr int kScanRunVectors = 1;
 
 enum : uint32_t { kFlagInvalid = 0, kFlagAggregate = 1, kFlagPrefix = 2 };
 
@@ -368,24 +371,36 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   const size_t tile_vec0 = tile * size_t(THREADS) * V;
   const size_t warp_vec0 = tile_vec0 + size_t(warp) * kWarp * V;
 
-  constexpr int G = (16 / N) < V ? (16 / N) : V;  // chunks loaded together (16 elements)
-  Acc lane_pre[V];  // prefix of this lane's first element within the warp's part of the tile
+  // A lane owns R consecutive vectors per chunk (its serial run); a warp's
+  // chunk is 32*R consecutive vectors; G chunks are loaded together.
+  constexpr int R = kScanRunVectors < V ? kScanRunVectors : V;
+  static_assert(V % R == 0, "whole runs per thread");
+  constexpr int CH = V / R;
+  constexpr int G0 = (16 / N) / R > 0 ? (16 / N) / R : 1;
+  constexpr int G = G0 < CH ? G0 : CH;
+  static_assert(CH % G == 0, "whole groups per thread");
+  Acc lane_pre[CH];  // prefix of this lane's first element within the warp's part of the tile
   Acc run = P::ident();
   const bool interior = (warp_vec0 * N >= head_pad) && (warp_vec0 + size_t(V) * kWarp) * N <= nv;
 #pragma unroll
-  for (int g = 0; g < V; g += G) {
-    T x[G][N];
+  for (int g = 0; g < CH; g += G) {
+    T x[G][R][N];
 #pragma unroll
     for (int c = 0; c < G; ++c)
-      load_chunk_l2<T>(in, warp_vec0 + size_t(g + c) * kWarp + lane, head_pad, nv, vec_ok != 0, x[c]);
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+        load_chunk_l2<T>(in, warp_vec0 + size_t(g + c) * kWarp * R + size_t(lane) * R + q, head_pad, nv,
+                         vec_ok != 0, x[c][q]);
 #pragma unroll
     for (int c = 0; c < G; ++c) {
       const int j = g + c;
-      const size_t u0 = (warp_vec0 + size_t(j) * kWarp + lane) * N;
+      const size_t u0 = (warp_vec0 + size_t(j) * kWarp * R + size_t(lane) * R) * N;
       Acc t = P::ident();
 #pragma unroll
-      for (int k = 0; k < N; ++k)
-        if (interior || (u0 + k >= head_pad && u0 + k < nv)) t = P::add(t, x[c][k]);
+      for (int q = 0; q < R; ++q)
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          if (interior || (u0 + q * N + k >= head_pad && u0 + q * N + k < nv)) t = P::add(t, x[c][q][k]);
       Acc incl = t;
 #pragma unroll
       for (int d = 1; d < kWarp; d <<= 1) {
@@ -424,38 +439,44 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   const Acc base = P::comb(P::from_carry(tile_prefix), warp_excl);
   T *vout_base = out - head_pad;
 #pragma unroll
-  for (int g = 0; g < V; g += G) {
-    T x[G][N];
+  for (int g = 0; g < CH; g += G) {
+    T x[G][R][N];
 #pragma unroll
     for (int c = 0; c < G; ++c)
-      load_chunk<T>(in, warp_vec0 + size_t(g + c) * kWarp + lane, head_pad, nv, vec_ok != 0, x[c]);
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+        load_chunk<T>(in, warp_vec0 + size_t(g + c) * kWarp * R + size_t(lane) * R + q, head_pad, nv, vec_ok != 0,
+                      x[c][q]);
 #pragma unroll
     for (int c = 0; c < G; ++c) {
       const int j = g + c;
-      const size_t vi = warp_vec0 + size_t(j) * kWarp + lane;
-      const size_t u0 = vi * N;
       Acc r = P::comb(base, lane_pre[j]);
-      T y[N];
 #pragma unroll
-      for (int k = 0; k < N; ++k) {
-        const bool ok = interior || (u0 + k >= head_pad && u0 + k < nv);
-        if (exclusive) {
-          y[k] = P::out(r);
-          if (ok) r = P::add(r, x[c][k]);
-        } else {
-          if (ok) r = P::add(r, x[c][k]);
-          y[k] = P::out(r);
+      for (int q = 0; q < R; ++q) {
+        const size_t vi = warp_vec0 + size_t(j) * kWarp * R + size_t(lane) * R + q;
+        const size_t u0 = vi * N;
+        T y[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+          const bool ok = interior || (u0 + k >= head_pad && u0 + k < nv);
+          if (exclusive) {
+            y[k] = P::out(r);
+            if (ok) r = P::add(r, x[c][q][k]);
+          } else {
+            if (ok) r = P::add(r, x[c][q][k]);
+            y[k] = P::out(r);
+          }
         }
-      }
-      if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
-        vec16<T> w;
+        if (vec_ok && u0 >= head_pad && u0 + N <= nv) {
+          vec16<T> w;
 #pragma unroll
-        for (int k = 0; k < N; ++k) w.v[k] = y[k];
-        st_stream16(reinterpret_cast<vec16<T> *>(vout_base) + vi, w);
-      } else {
+          for (int k = 0; k < N; ++k) w.v[k] = y[k];
+          st_stream16(reinterpret_cast<vec16<T> *>(vout_base) + vi, w);
+        } else {
 #pragma unroll
-        for (int k = 0; k < N; ++k)
-          if (u0 + k >= head_pad && u0 + k < nv) vout_base[u0 + k] = y[k];
+          for (int k = 0; k < N; ++k)
+            if (u0 + k >= head_pad && u0 + k < nv) vout_base[u0 + k] = y[k];
+        }
       }
     }
   }
