@@ -46,7 +46,7 @@ namespace {
 constexpr int kScanThreads = 256;
 // 16-byte vectors a lane owns consecutively per chunk (its serial run before
 // the chunk's warp scan).
-constexpr int kScanRunVectors = 1;
+constexpr int kScanRunVectors = 2;
 
 enum : uint32_t { kFlagInvalid = 0, kFlagAggregate = 1, kFlagPrefix = 2 };
 

@@ -168,7 +168,7 @@ __global__ void seg_tile_first_kernel(const unsigned long long *__restrict__ off
 
 // Bytes of consecutive elements a lane owns per chunk of the segmented scan
 // (a multiple of 16: one or more 16-byte vector loads).
-constexpr int kSegRunBytes = 16;
+constexpr int kSegRunBytes = 32;
 
 template <class T, int N>
 struct alignas(sizeof(T) * N) SegVec {
