@@ -213,6 +213,8 @@ __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t *p) {
 // bcx_device_error_check().
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr uint32_t kErrLookbackTimeout = 1u;
+// A bulk copy into shared memory did not complete within kSpinLimit polls.
+constexpr uint32_t kErrCopyTimeout = 2u;
 
 __device__ __forceinline__ void report_error(uint32_t *err, uint32_t code) {
   if (err) atomicOr(err, code);
@@ -278,6 +280,23 @@ __device__ __forceinline__ void bulk_load_smem(void *dst, const void *src, uint3
                    smem_addr(dst)),
                "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
+}
+// Bulk prefetch of global memory into L2 (no completion to wait for).  Same
+// rules: 16-byte aligned start, a multiple of 16 bytes.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+// Bulk copy from shared memory to global memory, tracked by bulk groups: the
+// issuing thread commits the group and waits until the copy has finished
+// reading shared memory before that memory may be released or rewritten.
+__device__ __forceinline__ void bulk_store_global(void *dst, const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit_group() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_group_read0() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 // Bounded wait for phase `parity` of `bar`; false if the limit was reached.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity) {

@@ -6,24 +6,27 @@
 // ~12 launches at 2^30).  Exclusive output[0] = init (:59-66); in-place scans
 // go through a temporary copy (:281-308).
 //
-// GB300 design: single-pass decoupled look-back.  Each 256-thread block takes
-// the next tile from an atomic ticket (so a block only ever waits on tiles
-// that were handed out before it, which guarantees forward progress) and
-// reads its tile with 16-byte loads (warp w owns a contiguous 32*V-vector run;
-// in chunk j lane l owns vector j*32 + l, so every load and store is fully
-// coalesced).  The first read (cached in L2, not L1) only produces each lane's
-// prefix per chunk by warp shuffles and the tile's aggregate, which is
-// published; warp 0 then looks back over 32 predecessors at a time for the
-// nearest inclusive prefix.  The tile is read a second time for the outputs:
-// it was read microseconds earlier, so that read is served by the 129 MB L2,
-// and keeping no tile data in registers across the look-back lets four 64 KB
-// tiles stay resident per SM, which hides the look-back latency.  DRAM still
-// sees 8 bytes per element.  In-place scans need no copy: a tile reads all of
-// its input (both times) before writing any output -- the second read of a
-// chunk precedes its own write, and other tiles never touch it.  Inputs that
-// fit one tile run as one launch with no look-back.  Every wait on a
-// predecessor is bounded (kSpinLimit polls); on expiry the block records
-// BCX_DEVICE_TIMEOUT and continues.
+// GB300 design: single-pass decoupled look-back over tiles staged in shared
+// memory.  Each 256-thread block takes the next tile from an atomic ticket (so
+// a block only ever waits on tiles that were handed out before it, which
+// guarantees forward progress) and moves the whole tile (64 KB; 96 KB for
+// 8-byte elements) into shared memory with bulk asynchronous copies completed
+// on an mbarrier, while asking L2 to prefetch the tile 16 MB further on.  Each
+// thread folds its contiguous run of the tile from shared memory, a block scan
+// of the run totals gives the tile aggregate, which is published; warp 0 looks
+// back over 32 predecessors at a time for the nearest inclusive prefix; each
+// thread then rewrites its run in place with its outputs, and bulk copies move
+// the tile out.  DRAM sees 8 bytes per element and nothing is re-read.
+// In-place scans need no copy: a tile is read whole before any of it is
+// written, and other tiles never touch it.
+//
+// Inputs that fit one tile, and inputs or outputs that are not 16-byte
+// aligned (bulk copies need that), take a register-tiled form instead: 16-byte
+// loads with lane runs per warp chunk, a first read (cached in L2) that only
+// forms per-lane prefixes and the aggregate, and a second read for the
+// outputs after the look-back.  Every wait on a predecessor or on a bulk copy
+// is bounded (kSpinLimit polls); on expiry the block records a device error
+// and finishes.
 //
 // Float plus with compensated=1 keeps Neumaier (s, c) pairs for every sum
 // inside a tile and carries tile prefixes between blocks in FP64.
@@ -482,6 +485,205 @@ scan_tile_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, size_t
   }
 }
 
+// ---- shared-memory staged tiles --------------------------------------------
+// Tile bytes of the staged scan (three resident tiles per SM) and the size of
+// each bulk copy that moves a tile in or out.
+constexpr uint32_t kStagedPieceBytes = 16 * 1024;
+constexpr int kStagedThreads = 256;
+// Tile bytes (measured on GB300 at 2^30 elements): 64 KB, three resident per
+// SM; 96 KB for 8-byte elements, whose fenced status words make each look-back
+// step dearer, so fewer and larger tiles pay (2.08 ms against 2.40 ms for an
+// int64 scan of 2^30 elements).
+template <class T> struct staged_tile_bytes {
+  static constexpr uint32_t value = sizeof(T) == 8 ? 96u * 1024u : 64u * 1024u;
+};
+// A block that takes tile i asks L2 to prefetch the tile kStagedPrefetchBytes
+// further on, so by the time that tile's block starts, its bulk load is served
+// from L2: short, even load times keep the look-back waits short (they wait
+// for the slowest predecessor's load), and the DRAM latency is absorbed by the
+// 129 MB L2 rather than by shared memory held idle.  16 MB ahead took a 2^30
+// int32 scan from 2.02 ms to 1.63 ms; 32 MB and more ahead gained nothing.
+constexpr size_t kStagedPrefetchBytes = size_t(16) << 20;
+// Resident tiles per SM that the shared memory allows (1 KB per block is
+// reserved by the hardware; at most 8 blocks are asked for).
+constexpr int staged_blocks_per_sm(uint32_t tile_bytes) {
+  return int((227u * 1024u) / (tile_bytes + 1024u)) < 8 ? int((227u * 1024u) / (tile_bytes + 1024u)) : 8;
+}
+
+// One block = one tile of TILE_BYTES, moved into shared memory by bulk
+// copies (the whole tile in flight at once, no registers held for it) and
+// out again by bulk copies after the scan.  Thread t owns the contiguous run
+// of VPT 16-byte vectors starting at vector t*VPT.  A thread visits its
+// vectors starting at vector (t mod VPT) and wrapping around, so the eight
+// threads of each shared-memory phase touch eight different bank groups; the
+// fold still combines the run in element order: `part_a` holds vectors
+// [r, VPT) and `part_b` vectors [0, r), and the run total is part_b op part_a.
+// The second pass rewrites the run in place with its outputs.  DRAM sees each
+// input byte once and each output byte once; L2 sees no re-read.
+template <class T, class P, class Status, uint32_t TILE_BYTES = staged_tile_bytes<T>::value>
+__global__ void __launch_bounds__(kStagedThreads, staged_blocks_per_sm(TILE_BYTES))
+scan_staged_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n, int exclusive,
+                   typename P::Carry init_carry, Status st, uint32_t *tile_counter, uint32_t *err) {
+  typedef typename P::Acc Acc;
+  typedef typename P::Carry Carry;
+  constexpr int N = 16 / sizeof(T);
+  constexpr int VPT = int(TILE_BYTES / (kStagedThreads * 16u));
+  constexpr int ITEMS = VPT * N;
+  constexpr uint32_t TILE = uint32_t(kStagedThreads) * ITEMS;
+  constexpr int WARPS = kStagedThreads / kWarp;
+  constexpr size_t PREFETCH_TILES = kStagedPrefetchBytes / TILE_BYTES;
+  static_assert(VPT >= 1 && TILE_BYTES % kStagedPieceBytes == 0, "whole pieces per tile");
+  extern __shared__ __align__(128) unsigned char staged_smem[];
+  vec16<T> *tv = reinterpret_cast<vec16<T> *>(staged_smem);
+  T *te = reinterpret_cast<T *>(staged_smem);
+  __shared__ unsigned long long bar;
+  __shared__ Acc warp_tot[WARPS];
+  __shared__ Carry tile_prefix;
+  __shared__ uint32_t tile_slot;
+
+  if (threadIdx.x == 0) {
+    tile_slot = atomicAdd(tile_counter, 1u);
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const size_t tile = tile_slot;
+  const size_t base = tile * TILE;
+  const uint32_t cnt = uint32_t((n - base) < TILE ? (n - base) : TILE);
+  const uint32_t bulk = (cnt * uint32_t(sizeof(T))) & ~15u;
+  const uint32_t bulk_elems = bulk / uint32_t(sizeof(T));
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(&bar, bulk);
+    const char *src = reinterpret_cast<const char *>(in + base);
+    for (uint32_t off = 0; off < bulk; off += kStagedPieceBytes)
+      bulk_load_smem(staged_smem + off, src + off, (bulk - off) < kStagedPieceBytes ? (bulk - off) : kStagedPieceBytes,
+                     &bar);
+    const size_t ahead = tile + PREFETCH_TILES;
+    if (PREFETCH_TILES > 0 && ahead * TILE < n) {
+      const size_t rest = n - ahead * TILE;
+      const uint32_t pf = uint32_t((rest < TILE ? rest : size_t(TILE)) * sizeof(T)) & ~15u;
+      const char *pfs = reinterpret_cast<const char *>(in + ahead * TILE);
+      for (uint32_t off = 0; off < pf; off += kStagedPieceBytes)
+        bulk_prefetch_l2(pfs + off, (pf - off) < kStagedPieceBytes ? (pf - off) : kStagedPieceBytes);
+    }
+  }
+  // The last tile's ragged end (under 16 bytes) comes in by plain loads.
+  for (uint32_t i = bulk_elems + threadIdx.x; i < cnt; i += kStagedThreads) te[i] = in[base + i];
+  const bool arrived = mbar_wait_bounded(&bar, 0);
+  if (__syncthreads_or(!arrived)) {
+    // Leave only after the copies into this block's shared memory are done.
+    if (threadIdx.x == 0) {
+      report_error(err, kErrCopyTimeout);
+      mbar_wait_bounded(&bar, 0);
+    }
+    return;
+  }
+
+  const unsigned t = threadIdx.x, lane = lane_id(), warp = t / kWarp;
+  const bool full = (cnt == TILE);
+  const uint32_t e_first = t * uint32_t(ITEMS);
+  const int r = int(t % unsigned(VPT));
+  Acc a = P::ident(), part_a = P::ident();
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    int v = k + r;
+    if (v >= VPT) v -= VPT;
+    if (k > 0 && v == 0) {
+      part_a = a;
+      a = P::ident();
+    }
+    const vec16<T> x = tv[t * VPT + v];
+#pragma unroll
+    for (int m = 0; m < N; ++m)
+      if (full || e_first + uint32_t(v * N + m) < cnt) a = P::add(a, x.v[m]);
+  }
+  Acc part_b = P::ident();
+  if (r == 0) part_a = a;
+  else part_b = a;
+  // Block scan of the run totals.
+  Acc incl = P::comb(part_b, part_a);
+#pragma unroll
+  for (int d = 1; d < kWarp; d <<= 1) {
+    const Acc o = P::shfl_up(incl, d);
+    if (int(lane) >= d) incl = P::comb(o, incl);
+  }
+  Acc lane_excl = P::shfl_up(incl, 1);
+  if (lane == 0) lane_excl = P::ident();
+  if (lane == kWarp - 1) warp_tot[warp] = incl;
+  __syncthreads();
+  Acc warp_excl = P::ident(), tile_agg = P::ident();
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) {
+    if (w == int(warp)) warp_excl = tile_agg;
+    tile_agg = P::comb(tile_agg, warp_tot[w]);
+  }
+  if (warp == 0) {
+    const Carry first_prefix = exclusive ? init_carry : P::carry_ident();
+    Carry pre;
+    if (tile == 0) {
+      pre = first_prefix;
+      if (lane == 0) st.publish(0, kFlagPrefix, P::carry_comb(first_prefix, P::to_carry(tile_agg)));
+    } else {
+      pre = lookback<P>(st, tile, P::to_carry(tile_agg), err);
+    }
+    if (lane == 0) tile_prefix = pre;
+  }
+  __syncthreads();
+  const Acc pre = P::comb(P::comb(P::from_carry(tile_prefix), warp_excl), lane_excl);
+  Acc run = P::comb(pre, part_b);
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    int v = k + r;
+    if (v >= VPT) v -= VPT;
+    if (k > 0 && v == 0) run = pre;
+    const vec16<T> x = tv[t * VPT + v];
+    vec16<T> y;
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      const bool ok = full || e_first + uint32_t(v * N + m) < cnt;
+      if (exclusive) {
+        y.v[m] = P::out(run);
+        if (ok) run = P::add(run, x.v[m]);
+      } else {
+        if (ok) run = P::add(run, x.v[m]);
+        y.v[m] = P::out(run);
+      }
+    }
+    tv[t * VPT + v] = y;
+  }
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    char *dst = reinterpret_cast<char *>(out + base);
+    for (uint32_t off = 0; off < bulk; off += kStagedPieceBytes)
+      bulk_store_global(dst + off, staged_smem + off, (bulk - off) < kStagedPieceBytes ? (bulk - off) : kStagedPieceBytes);
+    bulk_commit_group();
+    bulk_wait_group_read0();
+  }
+  for (uint32_t i = bulk_elems + threadIdx.x; i < cnt; i += kStagedThreads) out[base + i] = te[i];
+}
+
+// Opts scan_staged_kernel<T, P, Status> into its tile bytes of dynamic
+// shared memory on the current device (once per device and instantiation:
+// the flags are per instantiation, not per kernel signature, which several
+// functors share).
+template <class T, class P, class Status>
+cudaError_t staged_smem_optin() {
+  auto kernel = scan_staged_kernel<T, P, Status>;
+  static std::mutex mu;
+  static uint64_t done = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 64 && (done >> dev) & 1u) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(staged_tile_bytes<T>::value));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
+  if (e == cudaSuccess && dev < 64) done |= uint64_t(1) << dev;
+  return e;
+}
+
 // Tile shape of the allocating scan (measured on GB300 at 2^30 elements):
 // 96 elements per thread when the accumulator is at most 4 bytes (96 KB tiles
 // of 4-byte elements; 64 and 128 per thread were slower), 32 compensated FP32
@@ -515,7 +717,12 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   const size_t tile_elems = size_t(THREADS) * V * N;
   const size_t tiles = div_up(nv, tile_elems);
   const bool single = (tiles <= 1);
-  const size_t need = single ? 0 : (256 + Status::bytes(tiles));
+  // Staged tiles need 16-byte aligned input and output (bulk copies); the
+  // temporary is sized for either shape, so a size query holds for both.
+  const size_t staged_tile_elems = staged_tile_bytes<T>::value / sizeof(T);
+  const size_t staged_tiles = div_up(n, staged_tile_elems);
+  const bool staged = !single && ((ain | aout) & 15u) == 0;
+  const size_t need = single ? 0 : (256 + Status::bytes(tiles > staged_tiles ? tiles : staged_tiles));
   TempStorage ts;
   bool query = false;
   rc = ts.acquire(temp, temp_bytes, need, s, &query);
@@ -533,6 +740,19 @@ bcx_status run_scan_t(cudaStream_t s, int exclusive, const void *init, const voi
   char *base = static_cast<char *>(ts.ptr());
   uint32_t *counter = reinterpret_cast<uint32_t *>(base);
   Status st;
+  if (staged) {
+    st.bind(base + 256, staged_tiles);
+    BCX_CUDA(cudaMemsetAsync(base, 0, 256, s));
+    BCX_CUDA(st.clear(staged_tiles, s));
+    BCX_CHECK(staged_tiles < (size_t(1) << 31), BCX_INVALID_VALUE, "scan: input too large");
+    BCX_CUDA((staged_smem_optin<T, P, Status>()));
+    auto kernel = scan_staged_kernel<T, P, Status>;
+    KernelScope ks("scan_lookback", s);
+    kernel<<<unsigned(staged_tiles), kStagedThreads, staged_tile_bytes<T>::value, s>>>(pin, pout, n, exclusive,
+                                                                                        init_carry, st,
+                                                                            counter, ds->err_word);
+    return launch_status("scan_lookback");
+  }
   st.bind(base + 256, tiles);
   BCX_CUDA(cudaMemsetAsync(base, 0, 256, s));
   BCX_CUDA(st.clear(tiles, s));
