@@ -286,6 +286,24 @@ __device__ __forceinline__ void bulk_load_smem(void *dst, const void *src, uint3
 __device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
+// Distance, in input bytes, at which the two-read tiled kernels (segmented
+// scan, reduce_by_key) ask L2 to prefetch the tile they will reach later: far
+// enough that the prefetch has landed when that tile's block starts, near
+// enough that it is still in L2 then.  Measured on GB300 at 2^28 elements:
+// 8 MB took reduce_by_key 1.28 -> 1.22 ms and segmented scan 0.51 -> 0.49 ms;
+// 32 MB was slower than none.
+constexpr size_t kL2PrefetchBytes = size_t(8) << 20;
+// Asks L2 to prefetch elements [first, first + count) of p, clipped to n.
+// p + first must be 16-byte aligned.
+template <class T>
+__device__ __forceinline__ void prefetch_l2_range(const T *p, size_t first, size_t count, size_t n) {
+  if (first >= n) return;
+  const size_t m = (n - first) < count ? (n - first) : count;
+  const uint32_t bytes = uint32_t(m * sizeof(T)) & ~15u;
+  const char *src = reinterpret_cast<const char *>(p + first);
+  for (uint32_t off = 0; off < bytes; off += 16384u)
+    bulk_prefetch_l2(src + off, (bytes - off) < 16384u ? (bytes - off) : 16384u);
+}
 // Bulk copy from shared memory to global memory, tracked by bulk groups: the
 // issuing thread commits the group and waits until the copy has finished
 // reading shared memory before that memory may be released or rewritten.

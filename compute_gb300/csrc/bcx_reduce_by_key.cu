@@ -276,6 +276,8 @@ __device__ __forceinline__ void load_run(const T *__restrict__ p, size_t e0, siz
   }
 }
 
+constexpr size_t kRbkPrefetchBytes = kL2PrefetchBytes;
+
 template <class K, class V, class P>
 __global__ void __launch_bounds__(kRbkThreads, 4)
 reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uint32_t n,
@@ -295,6 +297,15 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
     if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
     __syncthreads();
     tile = s_tile;
+    // Ask L2 for the keys and values of the tile kRbkPrefetchBytes ahead, so
+    // that tile's first read is served from L2 (short, even load times keep
+    // the look-back waits short).
+    if (kRbkPrefetchBytes > 0 && threadIdx.x == 0) {
+      const size_t ahead =
+          (size_t(tile) + kRbkPrefetchBytes / (size_t(Sh::TILE) * (sizeof(K) + sizeof(V)))) * size_t(Sh::TILE);
+      if ((reinterpret_cast<uintptr_t>(keys) & 15u) == 0) prefetch_l2_range(keys, ahead, Sh::TILE, n);
+      if ((reinterpret_cast<uintptr_t>(vals) & 15u) == 0) prefetch_l2_range(vals, ahead, Sh::TILE, n);
+    }
   }
   // Warp w covers CH chunks of 32*N consecutive elements; in chunk j lane l
   // owns elements chunk_base + l*N .. + N-1, so (j, l, m) is input order.

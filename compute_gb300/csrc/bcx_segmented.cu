@@ -178,6 +178,8 @@ struct alignas(sizeof(T) * N) SegVec {
 // ITEMS elements per thread in ITEMS/N chunks; in chunk j lane l owns the N
 // consecutive elements chunk_base + l*N .. + N-1 (one vector load and store
 // when the arrays are aligned), so (j, l, m) is input order within a warp.
+constexpr size_t kSegPrefetchBytes = kL2PrefetchBytes;
+
 template <class T, class P, int ITEMS>
 __global__ void __launch_bounds__(kSegThreads, 4)
 segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
@@ -200,6 +202,10 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
   __syncthreads();
   const size_t tile = s_tile;
   const size_t tile_base = tile * TILE;
+  // Ask L2 for the tile kSegPrefetchBytes ahead, so that tile's first read is
+  // served from L2 (short, even load times keep the look-back waits short).
+  if (kSegPrefetchBytes > 0 && threadIdx.x == 0 && vec_in)
+    prefetch_l2_range(in, (tile + kSegPrefetchBytes / (size_t(TILE) * sizeof(T))) * TILE, TILE, n);
   const size_t tile_end = (tile_base + TILE < n) ? tile_base + TILE : n;
   const uint32_t warp_first = warp * (kWarp * ITEMS);
   // Mark the segment starts inside this tile (offsets[0..nseg] are starts;
