@@ -272,6 +272,34 @@ def test_scan_integer_random(bc, cuda, dtype, op):
             np.testing.assert_array_equal(to_np(r, dtype), ref, err_msg=f"n={n} exclusive={exclusive}")
 
 
+# Tiles of the aligned (bulk-copy) scan: 64 KB, 96 KB for 8-byte elements.
+STAGED_TILE = {"uchar": 65536, "short": 32768, "int": 16384, "long": 12288}
+
+
+@pytest.mark.parametrize("dtype", list(STAGED_TILE))
+def test_scan_staged_ragged_tails(bc, cuda, dtype):
+    """Aligned inputs of several tiles whose last tile is whole, one element,
+    or a bulk-copied part plus a few trailing elements (under 16 bytes), in
+    place and out of place, against the oracle bit for bit."""
+    rng = np.random.default_rng(11)
+    t = STAGED_TILE[dtype]
+    w = np.dtype(NP[dtype]).itemsize
+    for n in [2 * t, 2 * t + 1, 3 * t + 1003 * (16 // w) + 3, 5 * t - 1]:
+        a = random_keys(rng, dtype, n)
+        for exclusive in (False, True):
+            d = to_dev(cuda, a, dtype)
+            if exclusive:
+                bc.exclusive_scan(d, out=d, init=NP[dtype](7), dtype=dtype)
+            else:
+                bc.inclusive_scan(d, out=d, dtype=dtype)
+            ref = oracle.scan(a, dtype, exclusive=exclusive, init=NP[dtype](7))
+            np.testing.assert_array_equal(to_np(d, dtype), ref, err_msg=f"n={n} exclusive={exclusive}")
+    x = rng.normal(1000.0, 1.0, size=3 * 16384 + 1003 * 4 + 3).astype(np.float32)
+    got = to_np(bc.inclusive_scan(to_dev(cuda, x, "float"), compensated=True), "float").astype(np.float64)
+    ref = oracle.prefix_f64(x, "float")
+    assert (np.abs(got - ref) / np.abs(ref)).max() <= 2.0 ** -23
+
+
 @pytest.mark.parametrize("offset", [0, 1, 2, 3])
 def test_scan_misaligned_and_inplace(bc, cuda, offset):
     rng = np.random.default_rng(offset)
