@@ -141,8 +141,8 @@ struct ScanCompF64 {
   }
 };
 
-// L2-coherent payload loads (issued after an acquire of the flag word).
-__device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
+// L2-coherent payload loads (issued after an acquire of the flag word).  FP64
+// carries need none: they live in self-validating words.
 __device__ __forceinline__ long long ldcg(const long long *p) { return __ldcg(p); }
 __device__ __forceinline__ unsigned long long ldcg(const unsigned long long *p) { return __ldcg(p); }
 __device__ __forceinline__ comp_f64 ldcg(const comp_f64 *p) {
