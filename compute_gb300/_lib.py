@@ -46,6 +46,13 @@ SIGNATURES = {
     "bcx_stream_create": (_i, [C.POINTER(_vp)]),
     "bcx_stream_destroy": (_i, [_vp]),
     "bcx_stream_synchronize": (_i, [_vp]),
+    "bcx_event_create": (_i, [C.POINTER(_vp)]),
+    "bcx_event_destroy": (_i, [_vp]),
+    "bcx_event_record": (_i, [_vp, _vp]),
+    "bcx_event_synchronize": (_i, [_vp]),
+    "bcx_event_query": (_i, [_vp, C.POINTER(_i)]),
+    "bcx_event_elapsed_ms": (_i, [_vp, _vp, C.POINTER(C.c_float)]),
+    "bcx_stream_wait_event": (_i, [_vp, _vp]),
     "bcx_malloc": (_i, [C.POINTER(_vp), _sz]),
     "bcx_free": (_i, [_vp]),
     "bcx_malloc_host": (_i, [C.POINTER(_vp), _sz]),

@@ -246,6 +246,59 @@ bcx_status bcx_stream_synchronize(bcx_stream stream) {
   return BCX_SUCCESS;
 }
 
+bcx_status bcx_event_create(bcx_event *event) {
+  BCX_CHECK(event != nullptr, BCX_INVALID_VALUE, "event is NULL");
+  cudaEvent_t e;
+  BCX_CUDA(cudaEventCreate(&e));
+  *event = (bcx_event)e;
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_event_destroy(bcx_event event) {
+  BCX_CHECK(event != nullptr, BCX_INVALID_VALUE, "event is NULL");
+  BCX_CUDA(cudaEventDestroy((cudaEvent_t)event));
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_event_record(bcx_event event, bcx_stream stream) {
+  BCX_CHECK(event != nullptr, BCX_INVALID_VALUE, "event is NULL");
+  BCX_CUDA(cudaEventRecord((cudaEvent_t)event, (cudaStream_t)stream));
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_event_synchronize(bcx_event event) {
+  BCX_CHECK(event != nullptr, BCX_INVALID_VALUE, "event is NULL");
+  BCX_CUDA(cudaEventSynchronize((cudaEvent_t)event));
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_event_query(bcx_event event, int *complete) {
+  BCX_CHECK(event != nullptr && complete != nullptr, BCX_INVALID_VALUE, "event or complete is NULL");
+  const cudaError_t e = cudaEventQuery((cudaEvent_t)event);
+  if (e == cudaErrorNotReady) {
+    // Not an error: the work before the event is still running.  Clear it from
+    // the runtime's last-error slot so a later launch check does not report it.
+    if (cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();
+    *complete = 0;
+    return BCX_SUCCESS;
+  }
+  BCX_CUDA(e);
+  *complete = 1;
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_event_elapsed_ms(bcx_event start, bcx_event end, float *ms) {
+  BCX_CHECK(start != nullptr && end != nullptr && ms != nullptr, BCX_INVALID_VALUE, "NULL argument");
+  BCX_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)end));
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_stream_wait_event(bcx_stream stream, bcx_event event) {
+  BCX_CHECK(event != nullptr, BCX_INVALID_VALUE, "event is NULL");
+  BCX_CUDA(cudaStreamWaitEvent((cudaStream_t)stream, (cudaEvent_t)event, 0));
+  return BCX_SUCCESS;
+}
+
 bcx_status bcx_malloc(void **ptr, size_t bytes) {
   BCX_CHECK(ptr != nullptr, BCX_INVALID_VALUE, "ptr is NULL");
   *ptr = nullptr;

@@ -89,6 +89,25 @@ bcx_status bcx_stream_create(bcx_stream *stream);
 bcx_status bcx_stream_destroy(bcx_stream stream);
 /* command_queue::finish() -- command_queue.hpp:1564 */
 bcx_status bcx_stream_synchronize(bcx_stream stream);
+/* Events: a marker recorded on a stream, completed when all work queued
+ * before it has finished; timing is enabled.  They replace the OpenCL events
+ * behind event.hpp (wait() :213, status() :173, duration via
+ * clGetEventProfilingInfo :202) and command_queue::enqueue_marker (:1622) /
+ * enqueue_barrier(wait_list) (:1601). */
+typedef void *bcx_event; /* a cudaEvent_t */
+bcx_status bcx_event_create(bcx_event *event);
+bcx_status bcx_event_destroy(bcx_event event);
+/* enqueue_marker: record `event` at the current end of `stream`. */
+bcx_status bcx_event_record(bcx_event event, bcx_stream stream);
+/* event::wait(): block the calling thread until the event has completed. */
+bcx_status bcx_event_synchronize(bcx_event event);
+/* event::status(): *complete = 1 when the event has completed, else 0. */
+bcx_status bcx_event_query(bcx_event event, int *complete);
+/* Milliseconds between two completed events recorded on the device. */
+bcx_status bcx_event_elapsed_ms(bcx_event start, bcx_event end, float *ms);
+/* enqueue_barrier(wait_list): later work on `stream` waits for `event`
+ * (on the device; the host does not block). */
+bcx_status bcx_stream_wait_event(bcx_stream stream, bcx_event event);
 /* buffer(context, size) -- buffer.hpp; freed by bcx_free */
 bcx_status bcx_malloc(void **ptr, size_t bytes);
 bcx_status bcx_free(void *ptr);

@@ -3,8 +3,11 @@
 #ifndef BOOST_COMPUTE_HPP
 #define BOOST_COMPUTE_HPP
 #include <boost/compute/algorithm.hpp>
+#include <boost/compute/async/future.hpp>
+#include <boost/compute/async/wait.hpp>
 #include <boost/compute/container/vector.hpp>
 #include <boost/compute/core.hpp>
+#include <boost/compute/event.hpp>
 #include <boost/compute/functional.hpp>
 #include <boost/compute/iterator/buffer_iterator.hpp>
 #include <boost/compute/iterator/counting_iterator.hpp>

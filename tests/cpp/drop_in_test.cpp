@@ -439,6 +439,73 @@ static void error_cases(compute::command_queue &q) {
   CHECK(thrown);
 }
 
+// copy_async / fill_async / futures / events.
+static void async_cases(compute::command_queue &q) {
+  // test_copy.cpp:219 copy_int_async
+  int host_data[] = {1, 2, 3, 4, 5, 6, 7, 8};
+  compute::vector<int> device_data(8, q.get_context());
+  compute::future<compute::vector<int>::iterator> h2d =
+      compute::copy_async(host_data, host_data + 8, device_data.begin(), q);
+  h2d.wait();
+  CHECK((to_host(device_data, q) == std::vector<int>{1, 2, 3, 4, 5, 6, 7, 8}));
+  CHECK(h2d.get() == device_data.end());
+  std::fill(host_data, host_data + 8, 0);
+  compute::future<int *> d2h = compute::copy_async(device_data.begin(), device_data.end(), host_data, q);
+  d2h.wait();
+  CHECK((std::vector<int>(host_data, host_data + 8) == std::vector<int>{1, 2, 3, 4, 5, 6, 7, 8}));
+  CHECK(d2h.get() == host_data + 8);
+
+  // test_async_wait.cpp:29 wait_for_copy: fill_async, then four pieces copied
+  // independently and waited for together
+  compute::vector<int> v(8, q.get_context());
+  compute::future<void> fill_future = compute::fill_async(v.begin(), v.end(), 9, q);
+  compute::wait_for_all(fill_future);
+  CHECK((to_host(v, q) == std::vector<int>(8, 9)));
+  int data[] = {1, 2, 3, 4, 5, 6, 7, 8};
+  auto c1 = compute::copy_async(data + 0, data + 2, v.begin() + 0, q);
+  auto c2 = compute::copy_async(data + 2, data + 4, v.begin() + 2, q);
+  auto c3 = compute::copy_async(data + 4, data + 6, v.begin() + 4, q);
+  auto c4 = compute::copy_async(data + 6, data + 8, v.begin() + 6, q);
+  compute::wait_for_all(c1, c2, c3, c4);
+  CHECK((to_host(v, q) == std::vector<int>{1, 2, 3, 4, 5, 6, 7, 8}));
+
+  // fill with a value whose bytes differ (doubling copies) and a ragged size
+  compute::vector<float> f(1000, q.get_context());
+  compute::fill(f.begin(), f.end(), 1.5f, q);
+  CHECK((to_host(f, q) == std::vector<float>(1000, 1.5f)));
+  compute::vector<int> pat(12345, q.get_context());
+  compute::fill_async(pat.begin(), pat.end(), 0x01020304, q).wait();
+  CHECK((to_host(pat, q) == std::vector<int>(12345, 0x01020304)));
+  compute::fill(pat.begin(), pat.end(), -1, q);  // one byte pattern: memset
+  CHECK((to_host(pat, q) == std::vector<int>(12345, -1)));
+
+  // page-locked host memory: the copy overlaps, its event times it, and a
+  // second queue waits for it on the device before reducing the data
+  const size_t n = size_t(1) << 24;
+  void *pinned = nullptr;
+  CHECK(bcx_malloc_host(&pinned, n * sizeof(int)) == BCX_SUCCESS);
+  if (pinned) {
+    int *hp = static_cast<int *>(pinned);
+    for (size_t i = 0; i < n; ++i) hp[i] = int(i % 7);
+    compute::vector<int> big(n, q.get_context());
+    compute::future<compute::vector<int>::iterator> up = compute::copy_async(hp, hp + n, big.begin(), q);
+    compute::command_queue q2(q.get_context(), compute::system::default_device());
+    up.get_event().enqueue_wait(q2);
+    int sum = 0;  // about 3 * 2^24: fits an int
+    compute::reduce(big.begin(), big.end(), &sum, q2);
+    up.wait();
+    CHECK(up.get_event().status() == compute::event::complete);
+    CHECK(up.get_event().duration<std::chrono::microseconds>().count() > 0);
+    int expect = 0;
+    for (size_t i = 0; i < n; ++i) expect += int(i % 7);
+    CHECK(sum == expect);
+    bcx_free_host(pinned);
+  }
+  compute::event never;  // never recorded: complete, and wait() returns
+  never.wait();
+  CHECK(never.status() == compute::event::complete);
+}
+
 int main() {
   compute::command_queue &q = compute::system::default_queue();
   readme_example();
@@ -453,6 +520,7 @@ int main() {
   comparator_sort_cases(q);
   compaction_cases(q);
   error_cases(q);
+  async_cases(q);
   q.check_device_errors();
   std::printf("%s (%d failures)\n", g_failures ? "FAILED" : "OK", g_failures);
   return g_failures ? 1 : 0;
