@@ -44,6 +44,10 @@
 #include "bcx_internal.h"
 
 namespace bcx {
+// Internal linkage on purpose: each translation unit that includes this header
+// instantiates the kernels it dispatches to as its own private copies, so no
+// kernel symbol or launch stub is shared between separately compiled device
+// images.
 namespace {
 
 // Block size of the allocating scan (the no-alloc entry point keeps its own
