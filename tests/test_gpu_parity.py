@@ -347,6 +347,32 @@ def test_reduce_random(bc, cuda, dtype, op):
         assert got == oracle.fold(a, dtype, op=op), f"n={n}"
 
 
+@pytest.mark.parametrize("dtype", ["float", "double"])
+@pytest.mark.parametrize("compensated", [False, True])
+def test_scan_float_types(bc, cuda, dtype, compensated):
+    """float / double scans, plain and compensated, one tile and several
+    (bulk-copy tiles: 16384 floats, 12288 doubles), against the FP64 oracle
+    prefix.  Tolerance per prefix: the worst-case bound of an arbitrary-order
+    sum in the element type, (i+1) * eps * sum|a[0..i]|; compensated sums
+    within 4 eps * sum|a[0..i]|."""
+    rng = np.random.default_rng(31)
+    eps = float(np.finfo(NP[dtype]).eps)
+    for n in [100, 3 * 16384 + 5]:
+        a = (rng.standard_normal(n) * 1000.0).astype(NP[dtype])
+        mag = np.cumsum(np.abs(a.astype(np.float64)))
+        bound = (4.0 * eps * mag) if compensated else (np.arange(1, n + 1) * eps * mag)
+        got = to_np(bc.inclusive_scan(to_dev(cuda, a, dtype), compensated=compensated, dtype=dtype),
+                    dtype).astype(np.float64)
+        ref = oracle.prefix_f64(a, dtype)
+        assert (np.abs(got - ref) <= bound + 1e-30).all(), f"inclusive n={n}"
+        got = to_np(bc.exclusive_scan(to_dev(cuda, a, dtype), init=2.5, compensated=compensated, dtype=dtype),
+                    dtype).astype(np.float64)
+        ref = oracle.prefix_f64(a, dtype, exclusive=True, init=2.5)
+        mag_x = np.concatenate([[2.5], 2.5 + mag[:-1]])
+        bound_x = (4.0 * eps * mag_x) if compensated else (np.arange(1, n + 1) * eps * mag_x)
+        assert (np.abs(got - ref) <= bound_x + 1e-30).all(), f"exclusive n={n}"
+
+
 def test_accumulate_float_compensated_accuracy(bc, cuda):
     """float accumulate of N(1000, 1): Neumaier in warps/blocks + FP64 combine
     lands within 1 ulp of the FP32 rounding of the FP64 sum; the reference's
