@@ -215,7 +215,7 @@ segsort_starts_kernel(const unsigned long long *__restrict__ offsets, const uint
   }
 }
 
-template <class U, int VB>
+template <class U, int VB, bool PLAIN>
 __global__ void __launch_bounds__(kSortThreads)
 segsort_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
                         typename value_type_of<VB>::type *__restrict__ vals_main,
@@ -223,7 +223,7 @@ segsort_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
                         const unsigned long long *__restrict__ offsets, uint32_t nseg,
                         const uint32_t *__restrict__ tile_first, const uint32_t *__restrict__ large_ord,
                         const uint32_t *__restrict__ totals, int pass, int passes, const KeyXform<U> xf,
-                        const uint32_t *__restrict__ digit_start, uint32_t *__restrict__ status,
+                        const uint32_t *__restrict__ digit_start, unsigned long long *__restrict__ status,
                         uint32_t *__restrict__ tile_counter, const uint32_t *__restrict__ tile_seg, uint32_t *err) {
   constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
   __shared__ uint32_t s_tile;
@@ -233,10 +233,10 @@ segsort_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
   if (t >= totals[0]) return;
   const LargeTile lt = tile_of_segment(offsets, tile_first, large_ord, tile_seg[t], t, TILE);
   const bool from_alt = (pass & 1) != 0;
-  onesweep_tile<U, VB>(from_alt ? keys_alt : keys_main, from_alt ? keys_main : keys_alt,
-                       from_alt ? vals_alt : vals_main, from_alt ? vals_main : vals_alt, lt.base, lt.count, t,
-                       lt.first_tile, digit_start + (size_t(lt.ord) * passes + pass) * kRadix, n,
-                       pass * kRadixBits, xf, status, err);
+  onesweep_tile<U, VB, PLAIN>(from_alt ? keys_alt : keys_main, from_alt ? keys_main : keys_alt,
+                              from_alt ? vals_alt : vals_main, from_alt ? vals_main : vals_alt, lt.base, lt.count, t,
+                              lt.first_tile, digit_start + (size_t(lt.ord) * passes + pass) * kRadix, n, pass,
+                              pass * kRadixBits, xf, status, err);
 }
 
 // Odd pass counts leave large segments in the temporary buffers.
@@ -407,8 +407,8 @@ SegLayout seg_layout(size_t n, size_t nseg) {
   off += 256;
   L.seg_hist = off;
   off += align256(size_t(L.max_large) * PASSES * kRadix * 4);
-  L.status = off;
-  off += align256(size_t(PASSES) * L.max_tiles * kRadix * 4);
+  L.status = off;  // one array for every pass (status words carry the pass)
+  off += align256(size_t(L.max_tiles) * kRadix * 8);
   L.total = off;
   L.zero_begin = L.counters;
   L.zero_bytes = off - L.counters;
@@ -441,6 +441,32 @@ bcx_status launch_small(cudaStream_t s, U *k_main, typename value_type_of<VB>::t
   }
 }
 
+template <class U, int VB, bool PLAIN>
+bcx_status seg_onesweep_passes(cudaStream_t s, const SegLayout &L, U *k_main, U *k_alt,
+                               typename value_type_of<VB>::type *v_main, typename value_type_of<VB>::type *v_alt,
+                               size_t n, const unsigned long long *offsets, size_t nseg, const uint32_t *tile_first,
+                               const uint32_t *large_ord, const uint32_t *totals, const KeyXform<U> &xf,
+                               const uint32_t *seg_hist, unsigned long long *status, uint32_t *counters,
+                               const uint32_t *tile_seg, uint32_t *err) {
+  constexpr int PASSES = int(sizeof(U));
+  constexpr size_t smem = OnesweepSmem<U, VB>::kBytes;
+  static bool attr = false;
+  if (!attr) {
+    BCX_CUDA(cudaFuncSetAttribute(segsort_onesweep_kernel<U, VB, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(smem)));
+    attr = true;
+  }
+  for (int p = 0; p < PASSES; ++p) {
+    KernelScope ks("segsort_onesweep", s);
+    segsort_onesweep_kernel<U, VB, PLAIN><<<L.max_tiles, kSortThreads, smem, s>>>(
+        k_main, k_alt, v_main, v_alt, uint32_t(n), offsets, uint32_t(nseg), tile_first, large_ord, totals, p, PASSES,
+        xf, seg_hist, status, counters + 1 + p, tile_seg, err);
+    bcx_status rc = launch_status("segsort_onesweep");
+    if (rc) return rc;
+  }
+  return BCX_SUCCESS;
+}
+
 template <class U, int VB>
 bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const unsigned long long *offsets,
                      size_t nseg, int kind, int desc, void *temp, size_t *temp_bytes) {
@@ -469,7 +495,7 @@ bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const u
   uint32_t *totals = reinterpret_cast<uint32_t *>(base + L.totals);
   uint32_t *counters = reinterpret_cast<uint32_t *>(base + L.counters);
   uint32_t *seg_hist = reinterpret_cast<uint32_t *>(base + L.seg_hist);
-  uint32_t *status = reinterpret_cast<uint32_t *>(base + L.status);
+  unsigned long long *status = reinterpret_cast<unsigned long long *>(base + L.status);
   const KeyXform<U> xf = make_xform<U>(kind, desc);
   const std::string obj = "segmented_sort_k" + std::to_string(8 * sizeof(U)) + "_v" + std::to_string(VB);
   uint32_t cap = param_get(obj, "small_tile", uint32_t(SmallCap<U, VB>::value));
@@ -501,21 +527,14 @@ bcx_status segsort_t(cudaStream_t s, void *keys, void *values, size_t n, const u
     rc = launch_status("segsort_starts");
     if (rc) return rc;
   }
-  constexpr size_t smem = OnesweepSmem<U, VB>::kBytes;
-  static bool attr2 = false;
-  if (!attr2) {
-    BCX_CUDA(cudaFuncSetAttribute(segsort_onesweep_kernel<U, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(smem)));
-    attr2 = true;
-  }
-  for (int p = 0; p < PASSES; ++p) {
-    KernelScope ks("segsort_onesweep", s);
-    segsort_onesweep_kernel<U, VB><<<L.max_tiles, kSortThreads, smem, s>>>(
-        k_main, k_alt, v_main, v_alt, uint32_t(n), offsets, uint32_t(nseg), tile_first, large_ord, totals, p,
-        PASSES, xf, seg_hist, status + size_t(p) * L.max_tiles * kRadix, counters + 1 + p, tile_seg, ds->err_word);
-    rc = launch_status("segsort_onesweep");
-    if (rc) return rc;
-  }
+  const bool plain = kind == kKeyUnsigned && !desc;
+  rc = plain ? seg_onesweep_passes<U, VB, true>(s, L, k_main, k_alt, v_main, v_alt, n, offsets, nseg, tile_first,
+                                                large_ord, totals, xf, seg_hist, status, counters, tile_seg,
+                                                ds->err_word)
+             : seg_onesweep_passes<U, VB, false>(s, L, k_main, k_alt, v_main, v_alt, n, offsets, nseg, tile_first,
+                                                 large_ord, totals, xf, seg_hist, status, counters, tile_seg,
+                                                 ds->err_word);
+  if (rc) return rc;
   if (PASSES & 1) {
     KernelScope ks("segsort_copyback", s);
     segsort_copyback_kernel<U, VB><<<L.max_tiles, 256, 0, s>>>(k_main, k_alt, v_main, v_alt, offsets,

@@ -17,12 +17,14 @@
 //      permutation: skipped, which keeps the result bit-identical), and
 //      decides which buffer each pass reads and writes;
 //   3. one kernel per 8-bit digit: each block takes the next tile from an
-//      atomic ticket, loads its keys (and values) warp-striped and fully
-//      coalesced, ranks them with __match_any_sync against per-warp digit
-//      counters in shared memory (stable: ranks follow input order), publishes
-//      its 256 digit counts, looks back over predecessor tiles per digit for
-//      the global offset (decoupled look-back, bounded waits), stages keys and
-//      values in shared memory in digit order and writes them out as runs of
+//      atomic ticket, loads its keys warp-striped and fully coalesced, ranks
+//      them within each warp against per-warp digit counters in shared memory
+//      (the lanes holding the same digit are found with one ballot per digit
+//      bit; stable: ranks follow input order), publishes its 256 digit counts,
+//      stages the keys in shared memory in digit order, issues the value
+//      loads, then looks back over predecessor tiles per digit for the global
+//      offset (decoupled look-back, 64-bit status words tagged with the pass,
+//      bounded waits), stages the values and writes the tile out as runs of
 //      consecutive addresses;
 //   4. if an odd number of passes ran, one copy kernel moves the result back.
 // Every launch is asynchronous on the caller's stream; nothing reads back to
@@ -142,15 +144,14 @@ radix_prep_kernel(uint32_t *__restrict__ hist, int passes, uint32_t n,
 
 // 3. One onesweep pass over digit `pass` (tiles taken from an atomic ticket,
 // so a tile only ever waits on tiles already running).
-template <class U, int VB>
-__global__ void __launch_bounds__(kSortThreads)
+template <class U, int VB, bool PLAIN>
+__global__ void __launch_bounds__(kSortThreads, kSortBlocksPerSm)
 radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
                       typename value_type_of<VB>::type *__restrict__ vals_main,
                       typename value_type_of<VB>::type *__restrict__ vals_alt, uint32_t n,
                       int pass, const KeyXform<U> xf, const uint32_t *__restrict__ digit_start,
-                      uint32_t *__restrict__ status, uint32_t *__restrict__ tile_counter,
+                      unsigned long long *__restrict__ status, uint32_t *__restrict__ tile_counter,
                       const SortControl *__restrict__ ctrl, uint32_t *err) {
-  typedef typename value_type_of<VB>::type VT;
   constexpr uint32_t TILE = OnesweepSmem<U, VB>::TILE;
   __shared__ uint32_t s_tile;
   if (ctrl->skip[pass]) return;
@@ -160,9 +161,9 @@ radix_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
   const uint32_t tile = s_tile;
   const uint32_t base = tile * TILE;
   const uint32_t count = (n - base) < TILE ? (n - base) : TILE;
-  onesweep_tile<U, VB>(from_alt ? keys_alt : keys_main, from_alt ? keys_main : keys_alt,
-                       from_alt ? vals_alt : vals_main, from_alt ? vals_main : vals_alt, base, count, tile, 0u,
-                       digit_start + pass * kRadix, n, pass * kRadixBits, xf, status, err);
+  onesweep_tile<U, VB, PLAIN>(from_alt ? keys_alt : keys_main, from_alt ? keys_main : keys_alt,
+                              from_alt ? vals_alt : vals_main, from_alt ? vals_main : vals_alt, base, count, tile,
+                              0u, digit_start + pass * kRadix, n, pass, pass * kRadixBits, xf, status, err);
 }
 
 // 4. Copy the result back when it ended in the temporary buffers.
@@ -234,12 +235,34 @@ SortLayout sort_layout(size_t n, size_t vb, int passes) {
   off += 256;
   L.counters = off;
   off += 256;
-  L.status = off;
-  off += align256(size_t(passes) * L.tiles * kRadix * 4);
+  L.status = off;  // one array for every pass (status words carry the pass)
+  off += align256(size_t(L.tiles) * kRadix * 8);
   L.total = off;
   L.zero_begin = L.hist;
   L.zero_bytes = off - L.hist;
   return L;
+}
+
+template <class U, int VB, bool PLAIN>
+bcx_status onesweep_passes(cudaStream_t s, const SortLayout &L, U *k_main, U *k_alt,
+                           typename value_type_of<VB>::type *v_main, typename value_type_of<VB>::type *v_alt,
+                           size_t n, const KeyXform<U> &xf, const uint32_t *hist, unsigned long long *status,
+                           uint32_t *counters, const SortControl *ctrl, uint32_t *err) {
+  const size_t smem = OnesweepSmem<U, VB>::kBytes;
+  static bool attr_set = false;
+  if (!attr_set) {
+    BCX_CUDA(cudaFuncSetAttribute(radix_onesweep_kernel<U, VB, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(smem)));
+    attr_set = true;
+  }
+  for (int p = 0; p < int(sizeof(U)); ++p) {
+    KernelScope ks("radix_onesweep", s);
+    radix_onesweep_kernel<U, VB, PLAIN><<<L.tiles, kSortThreads, smem, s>>>(
+        k_main, k_alt, v_main, v_alt, uint32_t(n), p, xf, hist, status, counters + p, ctrl, err);
+    bcx_status rc = launch_status("radix_onesweep");
+    if (rc) return rc;
+  }
+  return BCX_SUCCESS;
 }
 
 template <class U, int VB>
@@ -247,7 +270,7 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
                         void *temp, size_t *temp_bytes) {
   typedef typename value_type_of<VB>::type VT;
   constexpr int PASSES = int(sizeof(U));
-  BCX_CHECK(n < kMaxSortN, BCX_INVALID_VALUE, "radix sort: n must be below 2^30 (got %zu)", n);
+  BCX_CHECK(n <= kMaxSortN, BCX_INVALID_VALUE, "radix sort: n must be below 2^32 (got %zu)", n);
   DeviceState *ds = nullptr;
   bcx_status rc = current_device_state(&ds);
   if (rc) return rc;
@@ -265,7 +288,7 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
   uint32_t *hist = reinterpret_cast<uint32_t *>(base + L.hist);
   SortControl *ctrl = reinterpret_cast<SortControl *>(base + L.ctrl);
   uint32_t *counters = reinterpret_cast<uint32_t *>(base + L.counters);
-  uint32_t *status = reinterpret_cast<uint32_t *>(base + L.status);
+  unsigned long long *status = reinterpret_cast<unsigned long long *>(base + L.status);
   BCX_CUDA(cudaMemsetAsync(base + L.zero_begin, 0, L.zero_bytes, s));
   const KeyXform<U> xf = make_xform<U>(kind, desc);
   {
@@ -290,20 +313,12 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
     rc = launch_status("radix_prep");
     if (rc) return rc;
   }
-  const size_t smem = OnesweepSmem<U, VB>::kBytes;
-  static bool attr_set = false;
-  if (!attr_set) {
-    BCX_CUDA(cudaFuncSetAttribute(radix_onesweep_kernel<U, VB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    attr_set = true;
-  }
-  for (int p = 0; p < PASSES; ++p) {
-    KernelScope ks("radix_onesweep", s);
-    radix_onesweep_kernel<U, VB><<<L.tiles, kSortThreads, smem, s>>>(
-        k_main, k_alt, v_main, v_alt, uint32_t(n), p, xf, hist, status + size_t(p) * L.tiles * kRadix,
-        counters + p, ctrl, ds->err_word);
-    rc = launch_status("radix_onesweep");
-    if (rc) return rc;
-  }
+  const bool plain = kind == kKeyUnsigned && !desc;
+  rc = plain ? onesweep_passes<U, VB, true>(s, L, k_main, k_alt, v_main, v_alt, n, xf, hist, status, counters, ctrl,
+                                            ds->err_word)
+             : onesweep_passes<U, VB, false>(s, L, k_main, k_alt, v_main, v_alt, n, xf, hist, status, counters, ctrl,
+                                             ds->err_word);
+  if (rc) return rc;
   KernelScope ks("radix_copyback", s);
   size_t blocks = div_up(n, 256);
   size_t cap = size_t(ds->sm_count) * 8;
