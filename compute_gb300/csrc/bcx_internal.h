@@ -50,7 +50,7 @@ const char *dtype_name(bcx_dtype t);  // OpenCL C spelling: "int", "ulong", ...
 
 // Bytes rounded up to a 256-byte boundary (alignment of every sub-buffer
 // carved out of a temporary allocation).
-inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 // Temporary storage protocol shared by every algorithm entry point:
 //   temp == NULL && temp_bytes != NULL -> size query (returns 1 = "query done")
@@ -86,6 +86,13 @@ class KernelScope {
   cudaEvent_t start_ = nullptr;
 };
 bool profiling_enabled();
+
+// Reads and clears the error word of the no-alloc scan on the current device
+// (0 if that entry point never ran there).  Sets up no device state.
+bcx_status noalloc_take_error(uint32_t *word);
+// The library's state of the current device if an entry point has created it,
+// else nullptr (never creates it).
+DeviceState *existing_device_state();
 
 // Checks the launch that just happened.
 bcx_status launch_status(const char *kernel);

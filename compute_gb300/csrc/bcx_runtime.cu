@@ -79,6 +79,14 @@ bcx_status current_device_state(DeviceState **out) {
   return BCX_SUCCESS;
 }
 
+DeviceState *existing_device_state() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  auto it = g_devices.find(dev);
+  return it == g_devices.end() ? nullptr : it->second;
+}
+
 size_t dtype_size(bcx_dtype t) {
   switch (t) {
     case BCX_CHAR: case BCX_UCHAR: return 1;
@@ -312,6 +320,67 @@ bcx_status bcx_free(void *ptr) {
   return BCX_SUCCESS;
 }
 
+static std::mutex g_reg_mu;
+static std::map<void *, int> g_registered;  // host address -> registrations
+
+bcx_status bcx_host_register(void *host, size_t bytes, int read_only, void **device_ptr) {
+  BCX_CHECK(host != nullptr && device_ptr != nullptr && bytes > 0, BCX_INVALID_VALUE, "bad host registration");
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_registered.find(host);
+  if (it == g_registered.end()) {
+    unsigned flags = cudaHostRegisterMapped | cudaHostRegisterPortable;
+    if (read_only) flags |= cudaHostRegisterReadOnly;
+    BCX_CUDA(cudaHostRegister(host, bytes, flags));
+    it = g_registered.emplace(host, 0).first;
+  }
+  cudaError_t e = cudaHostGetDevicePointer(device_ptr, host, 0);
+  if (e != cudaSuccess) {
+    if (it->second == 0) {
+      cudaHostUnregister(host);
+      g_registered.erase(it);
+    }
+    return cuda_status(e, "cudaHostGetDevicePointer");
+  }
+  it->second += 1;
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_host_unregister(void *host) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_registered.find(host);
+  BCX_CHECK(it != g_registered.end(), BCX_INVALID_VALUE, "host memory %p is not registered", host);
+  if (--it->second == 0) {
+    g_registered.erase(it);
+    BCX_CUDA(cudaHostUnregister(host));
+  }
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_malloc_async(void **ptr, size_t bytes, bcx_stream stream) {
+  BCX_CHECK(ptr != nullptr, BCX_INVALID_VALUE, "ptr is NULL");
+  *ptr = nullptr;
+  if (bytes == 0) return BCX_SUCCESS;
+  DeviceState *st = nullptr;
+  bcx_status rc = current_device_state(&st);  // keeps freed memory cached in the pool
+  if (rc) return rc;
+  BCX_CUDA(cudaMallocAsync(ptr, bytes, (cudaStream_t)stream));
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_free_async(void *ptr, bcx_stream stream) {
+  if (ptr) BCX_CUDA(cudaFreeAsync(ptr, (cudaStream_t)stream));
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_device_error_word(void **word) {
+  BCX_CHECK(word != nullptr, BCX_INVALID_VALUE, "NULL argument");
+  DeviceState *st = nullptr;
+  bcx_status rc = current_device_state(&st);
+  if (rc) return rc;
+  *word = st->err_word;
+  return BCX_SUCCESS;
+}
+
 bcx_status bcx_malloc_host(void **ptr, size_t bytes) {
   BCX_CHECK(ptr != nullptr, BCX_INVALID_VALUE, "ptr is NULL");
   *ptr = nullptr;
@@ -340,14 +409,20 @@ bcx_status bcx_memset_async(void *dst, int byte_value, size_t bytes, bcx_stream 
 }
 
 bcx_status bcx_device_error_check(bcx_stream stream) {
-  DeviceState *st = nullptr;
-  bcx_status rc = current_device_state(&st);
-  if (rc) return rc;
   BCX_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  // Both error words of the current device: the library's (if any entry point
+  // set up the device) and the no-alloc scan's (if it ran here).  Checking
+  // sets up nothing, so a caller of the no-alloc scan stays allocation-free.
   uint32_t word = 0;
-  BCX_CUDA(cudaMemcpy(&word, st->err_word, sizeof(word), cudaMemcpyDeviceToHost));
+  if (DeviceState *st = existing_device_state()) {
+    BCX_CUDA(cudaMemcpy(&word, st->err_word, sizeof(word), cudaMemcpyDeviceToHost));
+    if (word) BCX_CUDA(cudaMemset(st->err_word, 0, sizeof(uint32_t)));
+  }
+  uint32_t na = 0;
+  bcx_status rc = noalloc_take_error(&na);
+  if (rc) return rc;
+  word |= na;
   if (word) {
-    BCX_CUDA(cudaMemset(st->err_word, 0, sizeof(uint32_t)));
     BCX_CUDA(cudaDeviceSynchronize());
     set_error("a bounded device-side wait expired (error word 0x%x)", word);
     return BCX_DEVICE_TIMEOUT;

@@ -45,19 +45,34 @@ extern "C" bcx_status bcx_scan(bcx_stream stream, bcx_dtype type, bcx_op op, int
 // pool and forbids libraries from calling cudaMalloc, or a latency-critical
 // path where cudaMalloc/cudaFree (which may synchronize the device) is not
 // acceptable.  bcx_scan_noalloc serves them: its look-back scratch (the tile
-// ticket and the per-tile status words) lives in one fixed array compiled
-// into this library, so the call needs only the caller's input and output.
+// ticket and the per-tile status words) and its error word live in one fixed
+// array compiled into this library, so the call needs only the caller's input
+// and output.  It also leaves the library's per-device state alone (that state
+// allocates an error word and a stream and configures the default memory
+// pool the first time any other entry point runs on a device).
 //
-// The array is kNoAllocScratchBytes (4 MiB) on every GPU that loads the
-// library and stays allocated until the process exits.  All calls share it:
-// each call clears the part it uses on its own stream before the scan kernel
-// runs, so back-to-back calls are fine, but calls whose work overlaps on the
-// GPU (different streams, or different host threads) race on the array and
-// must be serialized by the caller.
+// The array is kNoAllocScratchBytes (5 MiB + 4 KiB) on every GPU that loads
+// the library and stays allocated until the process exits.  Its size covers
+// the per-call limits below with any input alignment; larger n is rejected.
+// All calls share it: each call clears the part it uses on its own stream
+// before the scan kernel runs, so back-to-back calls are fine, but calls whose
+// work overlaps on the GPU (different streams, or different host threads)
+// race on the array and must be serialized by the caller.
 namespace bcx {
 namespace {
 
-constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
+// Layout: [0, 128) tile ticket, cleared by every call; [128, 132) error word
+// (a bounded wait that expired), kept until bcx_device_error_check reads and
+// clears it; tile status words from byte 256.
+constexpr size_t kNoAllocHeader = 256;
+constexpr size_t kNoAllocErrOffset = 128;
+// Per-call limits, by the carry between tiles: 2^30 elements of 1-, 2- and
+// 4-byte types (4-byte carries); 2^28 of 8-byte types and compensated float
+// (8-byte carries); 2^27 of compensated double (16-byte carries).
+constexpr size_t kNoAllocMax4 = size_t(1) << 30;
+constexpr size_t kNoAllocMax8 = size_t(1) << 28;
+constexpr size_t kNoAllocMax16 = size_t(1) << 27;
+constexpr size_t kNoAllocScratchBytes = (size_t(5) << 20) + 4096;
 constexpr int kNoAllocThreads = 128;
 constexpr int kNoAllocVectorsPerThread = 4;
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[kNoAllocScratchBytes];
@@ -94,17 +109,26 @@ bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, c
   // Fixed tile shape, so the size limit of the fixed scratch array does not
   // move when the allocating scan is retuned.
   constexpr int V = kNoAllocVectorsPerThread;
-  DeviceState *ds = nullptr;
-  bcx_status rc = current_device_state(&ds);
-  if (rc) return rc;
+  constexpr size_t tile_elems = size_t(kNoAllocThreads) * V * N;
+  constexpr size_t max_n = sizeof(Carry) == 4 ? kNoAllocMax4 : (sizeof(Carry) == 8 ? kNoAllocMax8 : kNoAllocMax16);
+  // Worst case: max_n elements behind an unaligned head (one extra tile).
+  static_assert(kNoAllocHeader + Status::bytes((max_n + tile_elems - 1) / tile_elems + 1) <= kNoAllocScratchBytes,
+                "no-alloc scratch array too small for its documented limit");
+  if (n > max_n) {
+    set_error("bcx_scan_noalloc: n = %zu is above its limit of %zu elements for this type and functor "
+              "(the fixed scratch array is %zu bytes; use bcx_scan for more)",
+              n, max_n, kNoAllocScratchBytes);
+    return BCX_INVALID_BUFFER_SIZE;
+  }
   void *scratch = nullptr;
-  rc = noalloc_scratch(&scratch);
+  bcx_status rc = noalloc_scratch(&scratch);
   if (rc) return rc;
+  char *base = static_cast<char *>(scratch);
+  uint32_t *err = reinterpret_cast<uint32_t *>(base + kNoAllocErrOffset);
   const uintptr_t ain = reinterpret_cast<uintptr_t>(in), aout = reinterpret_cast<uintptr_t>(out);
   const bool elem_aligned = (ain % sizeof(T) == 0) && (aout % sizeof(T) == 0);
   const bool vec_ok = elem_aligned && ((ain & 15u) == (aout & 15u));
   const size_t head_pad = vec_ok ? (ain & 15u) / sizeof(T) : 0;
-  const size_t tile_elems = size_t(kNoAllocThreads) * V * N;
   const size_t tiles = div_up(n + head_pad, tile_elems);
   const Carry init_carry = P::host_carry(init);
   const T *pin = static_cast<const T *>(in);
@@ -113,33 +137,18 @@ bcx_status run_scan_noalloc_t(cudaStream_t s, int exclusive, const void *init, c
     Status st{};
     KernelScope ks("scan_single", s);
     scan_tile_kernel<T, P, kNoAllocThreads, V, true, Status><<<1, kNoAllocThreads, 0, s>>>(
-        pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, nullptr, ds->err_word);
+        pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, nullptr, err);
     return launch_status("scan_single");
   }
-  const size_t need = 256 + Status::bytes(tiles);
-  if (need > kNoAllocScratchBytes) {
-    // Largest n whose tile status still fits in the array.
-    size_t lo = 0, hi = tiles;
-    while (lo + 1 < hi) {
-      const size_t mid = (lo + hi) / 2;
-      if (256 + Status::bytes(mid) <= kNoAllocScratchBytes) lo = mid;
-      else hi = mid;
-    }
-    set_error("bcx_scan_noalloc: n = %zu needs %zu bytes of scratch, more than its fixed %zu bytes; "
-              "at most %zu elements of this type/functor per call (use bcx_scan for more)",
-              n, need, kNoAllocScratchBytes, lo * tile_elems - head_pad);
-    return BCX_INVALID_BUFFER_SIZE;
-  }
-  char *base = static_cast<char *>(scratch);
   uint32_t *counter = reinterpret_cast<uint32_t *>(base);
   Status st;
-  st.bind(base + 256, tiles);
-  // The array keeps the previous call's tickets and flags: clear them.
-  BCX_CUDA(cudaMemsetAsync(base, 0, 256, s));
+  st.bind(base + kNoAllocHeader, tiles);
+  // The array keeps the previous call's ticket and status words: clear them.
+  BCX_CUDA(cudaMemsetAsync(base, 0, kNoAllocErrOffset, s));
   BCX_CUDA(st.clear(tiles, s));
   KernelScope ks("scan_lookback", s);
   scan_tile_kernel<T, P, kNoAllocThreads, V, false, Status><<<unsigned(tiles), kNoAllocThreads, 0, s>>>(
-      pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, ds->err_word);
+      pin, pout, n, head_pad, vec_ok ? 1 : 0, exclusive, init_carry, st, counter, err);
   return launch_status("scan_lookback");
 }
 
@@ -176,6 +185,24 @@ bcx_status noalloc_float(cudaStream_t s, int op, int ex, const void *init, const
 }
 
 }  // namespace
+
+bcx_status noalloc_take_error(uint32_t *word) {
+  *word = 0;
+  int dev = 0;
+  BCX_CUDA(cudaGetDevice(&dev));
+  void *p = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    auto it = g_noalloc_ptr.find(dev);
+    if (it == g_noalloc_ptr.end()) return BCX_SUCCESS;  // never used on this device
+    p = it->second;
+  }
+  char *err = static_cast<char *>(p) + kNoAllocErrOffset;
+  BCX_CUDA(cudaMemcpy(word, err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  if (*word) BCX_CUDA(cudaMemset(err, 0, sizeof(uint32_t)));
+  return BCX_SUCCESS;
+}
+
 }  // namespace bcx
 
 extern "C" bcx_status bcx_scan_noalloc(bcx_stream stream, bcx_dtype type, bcx_op op, int exclusive,

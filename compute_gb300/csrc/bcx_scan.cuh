@@ -165,7 +165,7 @@ struct TileStatus;
 template <class Carry>
 struct TileStatus<Carry, true> {
   unsigned long long *words;
-  static size_t bytes(size_t tiles) { return align256(tiles * 8); }
+  static constexpr size_t bytes(size_t tiles) { return align256(tiles * 8); }
   static size_t zero_bytes(size_t tiles) { return bytes(tiles); }
   void bind(char *base, size_t) { words = reinterpret_cast<unsigned long long *>(base); }
   cudaError_t clear(size_t tiles, cudaStream_t s) const { return cudaMemsetAsync(words, 0, zero_bytes(tiles), s); }
@@ -189,7 +189,7 @@ struct TileStatus<Carry, false> {
   uint32_t *flags;
   Carry *agg;
   Carry *inc;
-  static size_t bytes(size_t tiles) {
+  static constexpr size_t bytes(size_t tiles) {
     return align256(tiles * 4) + 2 * align256(tiles * sizeof(Carry));
   }
   static size_t zero_bytes(size_t tiles) { return align256(tiles * 4); }
@@ -223,7 +223,7 @@ struct TileStatus<double, false> {
   unsigned long long *agg;
   unsigned long long *inc;
   static constexpr unsigned long long kUnset = ~0ull;
-  static size_t bytes(size_t tiles) { return 2 * align256(tiles * 8); }
+  static constexpr size_t bytes(size_t tiles) { return 2 * align256(tiles * 8); }
   void bind(char *base, size_t tiles) {
     agg = reinterpret_cast<unsigned long long *>(base);
     inc = reinterpret_cast<unsigned long long *>(base + align256(tiles * 8));
@@ -260,7 +260,8 @@ constexpr int kLookbackDepth = 4;
 
 template <class P, class Status>
 __device__ __forceinline__ typename P::Carry lookback(Status &st, size_t tile,
-                                                      typename P::Carry agg, uint32_t *err) {
+                                                      typename P::Carry agg, uint32_t *err,
+                                                      uint32_t limit = kSpinLimit) {
   typedef typename P::Carry C;
   const unsigned lane = lane_id();
   if (lane == 0) st.publish(tile, kFlagAggregate, agg);
@@ -284,7 +285,7 @@ __device__ __forceinline__ typename P::Carry lookback(Status &st, size_t tile,
       const long long t = pred - (long long)lane - (long long)kWarp * j;
       uint32_t spins = 0;
       while (f[j] == kFlagInvalid) {
-        if (++spins > kSpinLimit) {
+        if (++spins > limit) {
           gave_up = true;
           f[j] = kFlagPrefix;
           v[j] = P::carry_ident();
