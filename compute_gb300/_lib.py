@@ -55,11 +55,17 @@ SIGNATURES = {
     "bcx_stream_wait_event": (_i, [_vp, _vp]),
     "bcx_malloc": (_i, [C.POINTER(_vp), _sz]),
     "bcx_free": (_i, [_vp]),
+    "bcx_malloc_async": (_i, [C.POINTER(_vp), _sz, _vp]),
+    "bcx_free_async": (_i, [_vp, _vp]),
+    "bcx_host_register": (_i, [_vp, _sz, _i, C.POINTER(_vp)]),
+    "bcx_host_unregister": (_i, [_vp]),
     "bcx_malloc_host": (_i, [C.POINTER(_vp), _sz]),
     "bcx_free_host": (_i, [_vp]),
     "bcx_memcpy_async": (_i, [_vp, _vp, _sz, _vp]),
     "bcx_memset_async": (_i, [_vp, _i, _sz, _vp]),
     "bcx_device_error_check": (_i, [_vp]),
+    "bcx_device_error_word": (_i, [C.POINTER(_vp)]),
+    "bcx_debug_expire_wait": (_i, [_vp, _i, C.c_uint]),
     "bcx_radix_sort_keys": (_i, [_vp, _i, _vp, _sz, _i, _vp, _szp]),
     "bcx_radix_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _i, _vp, _szp]),
     "bcx_sort_keys": (_i, [_vp, _i, _vp, _sz, _i, _vp, _szp]),
@@ -78,6 +84,7 @@ SIGNATURES = {
     "bcx_segmented_sort_pairs": (_i, [_vp, _i, _sz, _vp, _vp, _sz, _vp, _sz, _i, _vp, _szp]),
     "bcx_server_create": (_i, [C.POINTER(_vp), _i, _sz]),
     "bcx_server_configure": (_i, [_vp, _sz, _sz, _sz]),
+    "bcx_server_inject_faults": (_i, [_vp, _sz, _i]),
     "bcx_server_submit": (_i, [_vp, C.c_void_p, C.POINTER(C.c_uint64)]),
     "bcx_server_wait": (_i, [_vp, C.c_uint64, C.POINTER(C.c_double)]),
     "bcx_server_wait_for": (_i, [_vp, C.c_uint64, C.c_double, C.POINTER(C.c_double)]),

@@ -111,6 +111,22 @@ bcx_status bcx_stream_wait_event(bcx_stream stream, bcx_event event);
 /* buffer(context, size) -- buffer.hpp; freed by bcx_free */
 bcx_status bcx_malloc(void **ptr, size_t bytes);
 bcx_status bcx_free(void *ptr);
+/* Temporaries of one algorithm call, in stream order: the reference creates
+ * each call's temporary buffers and releases them when the call returns
+ * (detail/scan_on_gpu.hpp:216, detail/radix_sort.hpp:333-336); here they come
+ * from the device's stream-ordered pool and are released in stream order, so
+ * neither call blocks the host. */
+bcx_status bcx_malloc_async(void **ptr, size_t bytes, bcx_stream stream);
+bcx_status bcx_free_async(void *ptr, bcx_stream stream);
+/* Host memory used in place as a buffer (buffer with CL_MEM_USE_HOST_PTR,
+ * buffer.hpp:60-90; the storage of mapped_view, container/mapped_view.hpp:
+ * 44-120): `bytes` of host memory at `host` are page-locked and mapped into the
+ * device's address space, and *device_ptr is the address kernels use (on a
+ * Grace host the GPU reads it over the CPU-GPU link).  read_only != 0 for
+ * memory the device only reads.  Registrations of the same address are
+ * counted; bcx_host_unregister releases one. */
+bcx_status bcx_host_register(void *host, size_t bytes, int read_only, void **device_ptr);
+bcx_status bcx_host_unregister(void *host);
 /* Page-locked host memory (allocator/pinned_allocator.hpp). */
 bcx_status bcx_malloc_host(void **ptr, size_t bytes);
 bcx_status bcx_free_host(void *ptr);
@@ -123,6 +139,14 @@ bcx_status bcx_memset_async(void *dst, int byte_value, size_t bytes, bcx_stream 
  * that expired in this library's kernels since the last check
  * (BCX_DEVICE_TIMEOUT), or BCX_SUCCESS. */
 bcx_status bcx_device_error_check(bcx_stream stream);
+/* Test hook for failure detection (no counterpart in the reference, which
+ * reports errors through exceptions only, exception/opencl_error.hpp:30):
+ * runs one of the library's bounded device-side waits -- which = 0 the
+ * onesweep digit look-back, 1 the scan tile look-back, 2 the bulk-copy
+ * mbarrier wait -- against a status word or barrier that nothing publishes,
+ * giving up after `polls` polls (1 .. 2^20).  The kernel returns normally and
+ * the next bcx_device_error_check reports BCX_DEVICE_TIMEOUT. */
+bcx_status bcx_debug_expire_wait(bcx_stream stream, int which, unsigned polls);
 
 /* ---- sort ---------------------------------------------------------------
  * Radix path of detail::radix_sort / radix_sort_by_key
@@ -301,6 +325,12 @@ bcx_status bcx_server_create(bcx_server **server, int slots, size_t memory_budge
  * elements and batch_count requests per batch (0 keeps a value). */
 bcx_status bcx_server_configure(bcx_server *server, size_t small_limit, size_t batch_elems,
                                 size_t batch_count);
+/* Test hook (no counterpart in the reference): admission sees
+ * `fake_free_bytes` of free device memory instead of the measured figure (0 =
+ * measure), and the next `fail_allocations` batches fail as if their device
+ * allocation had failed (their requests end with BCX_MEM_ALLOCATION_FAILURE;
+ * later requests are served normally). */
+bcx_status bcx_server_inject_faults(bcx_server *server, size_t fake_free_bytes, int fail_allocations);
 bcx_status bcx_server_submit(bcx_server *server, const bcx_request *request, uint64_t *ticket);
 /* Blocks until the request's results are in place (host or device buffers). */
 bcx_status bcx_server_wait(bcx_server *server, uint64_t ticket, double *latency_ms);
@@ -340,6 +370,11 @@ bcx_status bcx_jit_cache_configure(size_t capacity, int clear);
 /* Streaming multiprocessors of the current device (grid sizing of generated
  * kernels). */
 bcx_status bcx_device_sm_count(int *sm_count);
+/* Device address of the current device's error word: generated kernels with
+ * bounded waits record an expired wait there (atomicOr of 1), and
+ * bcx_device_error_check reports it.  (The reference reports errors through
+ * exceptions only, exception/opencl_error.hpp:30.) */
+bcx_status bcx_device_error_word(void **word);
 
 /* ---- tuning parameters and autotuner (detail::parameter_cache,
  *      detail/parameter_cache.hpp:38-110; the perf/ tuning programs that fill

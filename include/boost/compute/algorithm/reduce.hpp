@@ -59,6 +59,7 @@ inline void reduce(InputIterator first, InputIterator last, buffer_iterator<T> r
   detail::device_range<InputIterator> in(first, last, queue);
   detail::jit_reduce(f.defs(), f.print(), detail::cuda_type_name<T>::get(), sizeof(T), in.ptr, in.n, nullptr,
                      result.get_ptr(), queue);
+  if (!std::is_same<InputIterator, buffer_iterator<T> >::value) queue.finish();  // keep the temporary alive
 }
 
 template <class InputIterator, class T, class F,
@@ -77,10 +78,19 @@ template <class InputIterator, class T, class BinaryFunction, class = detail::no
 inline T accumulate(InputIterator first, InputIterator last, T init, BinaryFunction,
                     command_queue &queue = system::default_queue()) {
   typedef typename std::iterator_traits<InputIterator>::value_type IT;
-  static_assert(std::is_same<IT, T>::value, "accumulate: init must have the element type");
   if (first == last) return init;
   detail::device_range<InputIterator> in(first, last, queue);
   vector<T> tmp(1, queue.get_context());
+  if (!std::is_same<IT, T>::value) {
+    // init of another type than the elements: the reference's serial fold
+    // with a conversion to T at every step (accumulate.hpp:31-55).
+    const std::string s = BinaryFunction::source();  // spelled with a and b
+    std::string e;
+    for (char c : s) e += (c == 'a') ? std::string("_1") : (c == 'b') ? std::string("_2") : std::string(1, c);
+    detail::jit_serial_fold("", e, detail::cuda_type_name<T>::get(), sizeof(T), detail::cuda_type_name<IT>::get(),
+                            in.ptr, in.n, &init, tmp.data(), queue);
+    return tmp.begin().read(queue);
+  }
   const int comp = std::is_floating_point<T>::value && BinaryFunction::bcx_op == BCX_PLUS;
   detail::check(bcx_accumulate(queue.get(), bcx_dtype(detail::bcx_dtype_of<T>()), bcx_op(BinaryFunction::bcx_op),
                                in.ptr, in.n, &init, tmp.data(), comp, nullptr, nullptr));
@@ -88,7 +98,8 @@ inline T accumulate(InputIterator first, InputIterator last, T init, BinaryFunct
 }
 template <class InputIterator, class T>
 inline T accumulate(InputIterator first, InputIterator last, T init, command_queue &queue = system::default_queue()) {
-  return ::boost::compute::accumulate(first, last, init, plus<T>(), queue);
+  typedef typename std::iterator_traits<InputIterator>::value_type IT;
+  return ::boost::compute::accumulate(first, last, init, plus<IT>(), queue);
 }
 
 }  // namespace compute

@@ -24,6 +24,7 @@ scan(InputIterator first, InputIterator last, buffer_iterator<T> result, bool ex
   device_range<InputIterator> in(first, last, queue);
   jit_scan(f.defs(), f.print(), cuda_type_name<T>::get(), sizeof(T), in.ptr, result.get_ptr(), in.n, exclusive,
            &init, queue);
+  if (!std::is_same<InputIterator, buffer_iterator<T> >::value) queue.finish();  // keep the temporary alive
   return result + std::ptrdiff_t(in.n);
 }
 

@@ -78,6 +78,7 @@ inline void transform_reduce(InputIterator first, InputIterator last, buffer_ite
   detail::device_range<InputIterator> in(first, last, queue);
   detail::fused_transform_reduce<T, A, A>(in.ptr, static_cast<const A *>(nullptr), in.n, transform_function,
                                           reduce_function, result.get_ptr(), queue);
+  if (!std::is_same<InputIterator, buffer_iterator<A> >::value) queue.finish();  // keep the temporary alive
 }
 
 template <class InputIterator, class T, class UnaryTransformFunction, class BinaryReduceFunction>
@@ -102,6 +103,9 @@ inline void transform_reduce(InputIterator1 first1, InputIterator1 last1, InputI
   detail::device_range<InputIterator2> b(first2, first2 + std::ptrdiff_t(a.n), queue);
   detail::fused_transform_reduce<T, A, B>(a.ptr, b.ptr, a.n, transform_function, reduce_function, result.get_ptr(),
                                           queue);
+  if (!std::is_same<InputIterator1, buffer_iterator<A> >::value ||
+      !std::is_same<InputIterator2, buffer_iterator<B> >::value)
+    queue.finish();  // keep the temporaries alive
 }
 
 template <class InputIterator1, class InputIterator2, class T, class BinaryTransformFunction,

@@ -4,10 +4,11 @@
 // OpenCL C text through meta_kernel (detail/meta_kernel.hpp:270-401) and
 // builds it once per context (utility/program_cache.hpp).  This layer emits
 // CUDA C++ instead and hands it to bcx_jit_get_kernel (NVRTC + LRU/disk cache
-// inside libbcx).  Three kernel shapes cover the algorithms:
+// inside libbcx).  Three kernel shapes cover the algorithms, each one launch,
+// asynchronous on the caller's queue:
 //   transform: out[i] = EXPR(_1 = a[i], _2 = b[i])   (16-byte vector path)
-//   reduce:    per-block folds of OP, then one block folds the partials
-//   scan:      tile totals, one block scans them, tiles rescanned with carry
+//   fold:      per-block in-order folds of OP, the last block folds the partials
+//   scan:      single-pass decoupled look-back over ticketed tiles
 // OP and EXPR are the user's source; they must be associative where the
 // reference requires it (reduce.hpp:263-281 documents the same).
 #ifndef BOOST_COMPUTE_DETAIL_JIT_HPP
@@ -43,7 +44,23 @@ inline const char *jit_prelude() {
          "template <class T> __device__ __forceinline__ T pown(T x, int n) {\n"
          "  T r = T(1); bool neg = n < 0; unsigned m = neg ? unsigned(-n) : unsigned(n);\n"
          "  while (m) { if (m & 1u) r *= x; x *= x; m >>= 1; } return neg ? T(1) / r : r; }\n"
-         "__device__ __forceinline__ int popcount(unsigned x) { return __popc(x); }\n";
+         "__device__ __forceinline__ int popcount(unsigned x) { return __popc(x); }\n"
+         // qualified spellings of the same types in user function signatures
+         "namespace boost { namespace compute { typedef signed char char_; typedef unsigned char uchar_;\n"
+         "typedef short short_; typedef unsigned short ushort_; typedef int int_; typedef unsigned int uint_;\n"
+         "typedef long long long_; typedef unsigned long long ulong_; typedef float float_; typedef double double_;\n"
+         "typedef ::int2 int2_; typedef ::int4 int4_; typedef ::uint2 uint2_; typedef ::float2 float2_;\n"
+         "typedef ::float4 float4_; } }\nnamespace compute = ::boost::compute;\n"
+         // element N of a tuple struct or component N of a vector type
+         "template <int N, class T> __device__ __forceinline__ auto bcx_get(const T &t) {"
+         " return t.template bcx_at<N>(); }\n"
+         "#define BCX_VEC_GET(V, S) template <int N> __device__ __forceinline__ S bcx_get(const V &v) {"
+         " return N == 0 ? v.x : (N == 1 ? v.y : (N == 2 ? v.z : v.w)); }\n"
+         "#define BCX_VEC2_GET(V, S) template <int N> __device__ __forceinline__ S bcx_get(const V &v) {"
+         " return N == 0 ? v.x : v.y; }\n"
+         "BCX_VEC_GET(int4, int) BCX_VEC_GET(float4, float) BCX_VEC2_GET(int2, int) BCX_VEC2_GET(uint2, unsigned)\n"
+         "BCX_VEC2_GET(float2, float)\n"
+         "#define boost_tuple_get(x, n) bcx_get<n>(x)\n";
 }
 
 // Exact source literal of a host value.
@@ -105,11 +122,9 @@ inline unsigned grid_for(size_t work, unsigned block) {
 }
 
 // out[i] = EXPR, with _1 = a[i] and (binary) _2 = b[i].
-inline void jit_transform(const std::string &defs, const std::string &expr, const char *t0, const char *t1,
-                          const char *tout, size_t s0, size_t s1, size_t sout, const void *a, const void *b,
-                          void *out, size_t n, command_queue &queue) {
-  if (n == 0) return;
-  const bool binary = b != nullptr;
+inline std::string jit_transform_source(const std::string &defs, const std::string &expr, const char *t0,
+                                        const char *t1, const char *tout, size_t s0, size_t s1, size_t sout,
+                                        bool binary) {
   std::ostringstream src;
   src << jit_prelude() << defs << "\n"
       << "extern \"C\" __global__ void bcx_jit_transform(const " << t0 << " *__restrict__ a, const "
@@ -138,6 +153,16 @@ inline void jit_transform(const std::string &defs, const std::string &expr, cons
       << "    const auto _1 = a[i];\n"
       << (binary ? "    const auto _2 = b[i];\n" : "")
       << "    r[i] = (" << tout << ")(" << expr << ");\n  }\n}\n";
+  return src.str();
+}
+
+inline void jit_transform(const std::string &defs, const std::string &expr, const char *t0, const char *t1,
+                          const char *tout, size_t s0, size_t s1, size_t sout, const void *a, const void *b,
+                          void *out, size_t n, command_queue &queue) {
+  if (n == 0) return;
+  const bool binary = b != nullptr;
+  const bool same = s0 == sout && (!binary || s1 == sout) && 16 % sout == 0;
+  const std::string source = jit_transform_source(defs, expr, t0, t1, tout, s0, s1, sout, binary);
   unsigned long long nn = n, nvec = 0;
   if (same) {
     const size_t N = 16 / sout;
@@ -147,76 +172,276 @@ inline void jit_transform(const std::string &defs, const std::string &expr, cons
   }
   const void *bb = binary ? b : a;
   void *args[] = {(void *)&a, (void *)&bb, (void *)&out, (void *)&nn, (void *)&nvec};
-  jit_launch(src.str(), "bcx_jit_transform", grid_for(n / 4 + 1, 256), 256, queue, args);
+  jit_launch(source, "bcx_jit_transform", grid_for(n / 4 + 1, 256), 256, queue, args);
 }
 
-// result = init OP fold(load(i)) (has_init) or fold(load(i)); one value of
+// ---- shared pieces of the generated fold and scan kernels -----------------
+// Both are written for any element type T the user's functor works on
+// (built-in scalars, CUDA vector types, structs): values move between lanes
+// as 32-bit words, partial results carry a "has a value" flag instead of an
+// identity element (a user functor has none), and every combination keeps
+// the input order, so a functor need only be associative, as the reference
+// requires (reduce.hpp:263-281).
+inline std::string jit_common(const std::string &defs, const std::string &op, const char *t) {
+  std::ostringstream src;
+  src << jit_prelude() << defs << "\n"
+      << "typedef " << t << " T;\n"
+      << "__device__ __forceinline__ T bcx_op(const T &_1, const T &_2) { return (T)(" << op << "); }\n"
+      << R"BCX(
+#define BCX_WORDS ((sizeof(T) + 3) / 4)
+// Byte copy of a compile-time size (registers after unrolling).
+template <unsigned long long BYTES>
+__device__ __forceinline__ void bcx_copy(void *d, const void *s) {
+#pragma unroll
+  for (unsigned long long i = 0; i < BYTES; ++i)
+    static_cast<unsigned char *>(d)[i] = static_cast<const unsigned char *>(s)[i];
+}
+__device__ __forceinline__ void bcx_to_words(const T &v, unsigned (&w)[BCX_WORDS]) {
+#pragma unroll
+  for (int k = 0; k < (int)BCX_WORDS; ++k) w[k] = 0u;
+  bcx_copy<sizeof(T)>(w, &v);
+}
+__device__ __forceinline__ T bcx_from_words(const unsigned (&w)[BCX_WORDS]) {
+  T r;
+  bcx_copy<sizeof(T)>(&r, w);
+  return r;
+}
+// Read of a value another block wrote, from L2 (never a stale L1 line).
+__device__ __forceinline__ T bcx_ldcg(const T *p) {
+  T r;
+  if (sizeof(T) % 4 == 0) {
+    unsigned w[BCX_WORDS];
+#pragma unroll
+    for (int k = 0; k < (int)BCX_WORDS; ++k) w[k] = __ldcg(reinterpret_cast<const unsigned *>(p) + k);
+    bcx_copy<sizeof(T)>(&r, w);
+  } else {
+    unsigned char c[sizeof(T)];
+#pragma unroll
+    for (int k = 0; k < (int)sizeof(T); ++k) c[k] = __ldcg(reinterpret_cast<const unsigned char *>(p) + k);
+    bcx_copy<sizeof(T)>(&r, c);
+  }
+  return r;
+}
+__device__ __forceinline__ T bcx_shfl_up(const T &v, unsigned d) {
+  unsigned w[BCX_WORDS];
+  bcx_to_words(v, w);
+#pragma unroll
+  for (int k = 0; k < (int)BCX_WORDS; ++k) w[k] = __shfl_up_sync(0xffffffffu, w[k], d);
+  return bcx_from_words(w);
+}
+__device__ __forceinline__ T bcx_shfl_down(const T &v, unsigned d) {
+  unsigned w[BCX_WORDS];
+  bcx_to_words(v, w);
+#pragma unroll
+  for (int k = 0; k < (int)BCX_WORDS; ++k) w[k] = __shfl_down_sync(0xffffffffu, w[k], d);
+  return bcx_from_words(w);
+}
+__device__ __forceinline__ T bcx_shfl_idx(const T &v, int src) {
+  unsigned w[BCX_WORDS];
+  bcx_to_words(v, w);
+#pragma unroll
+  for (int k = 0; k < (int)BCX_WORDS; ++k) w[k] = __shfl_sync(0xffffffffu, w[k], src);
+  return bcx_from_words(w);
+}
+// (a, ha) followed by (b, hb) in input order.
+__device__ __forceinline__ void bcx_comb(T &a, int &ha, const T &b, int hb) {
+  if (hb) { a = ha ? bcx_op(a, b) : b; ha = 1; }
+}
+// In-order fold of one value per lane (lane order = input order, lanes with
+// h == 0 hold nothing); the result is returned in every lane.
+__device__ __forceinline__ T bcx_warp_fold(T v, int &h) {
+  const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+  for (unsigned d = 1; d < 32; d <<= 1) {
+    const T o = bcx_shfl_down(v, d);
+    const int oh = __shfl_down_sync(0xffffffffu, h, d);
+    if ((lane & (2 * d - 1)) == 0 && lane + d < 32) bcx_comb(v, h, o, oh);
+  }
+  h = __shfl_sync(0xffffffffu, h, 0);
+  return bcx_shfl_idx(v, 0);
+}
+)BCX";
+  return src.str();
+}
+
+// Elements per thread of the generated kernels: 64 bytes per thread, at
+// most 16 elements.
+inline int jit_items(size_t tsize) {
+  const size_t k = 64 / (tsize ? tsize : 1);
+  return int(k < 1 ? 1 : (k > 16 ? 16 : k));
+}
+
+// result = init OP fold(load(i)) (init given) or fold(load(i)); one value of
 // type T at `out` (device).  OP is an expression of (_1, _2); LOAD the body of
 // the element read, a function of a[i] (and b[i]) -- "return a[i];" for a
 // plain reduce, the transform function applied to a[i] (and b[i]) for a fused
 // transform_reduce, so the transformed values are never written out.
+//
+// One launch: each block folds a contiguous range of 256 x ITEMS element
+// tiles in order (a thread folds its run of ITEMS consecutive elements, a warp
+// folds its threads in lane order, warp 0 folds the warps), writes its
+// partial, and the last block to finish (a ticket taken after a fence) folds
+// the partials in block order with init.  Asynchronous on the queue: its
+// temporaries are stream-ordered and nothing waits for the device.
+inline std::string jit_fold_source(const std::string &defs, const std::string &op, const char *t, size_t tsize,
+                                   const std::string &load, const char *ta, const char *tb) {
+  const int items = jit_items(tsize);
+  std::ostringstream src;
+  src << jit_common(defs, op, t)
+      << "typedef " << ta << " TA;\n"
+      << "typedef " << (tb ? tb : ta) << " TB;\n"
+      << "#define BCX_ITEMS " << items << "\n"
+      << "__device__ __forceinline__ T bcx_load(const TA *__restrict__ a, const TB *__restrict__ b,"
+      << " unsigned long long i) { " << load << " }\n"
+      << R"BCX(
+extern "C" __global__ void __launch_bounds__(256)
+bcx_jit_fold(const TA *__restrict__ a, const TB *__restrict__ b, unsigned long long n, unsigned long long per_block,
+             T *__restrict__ part, int *__restrict__ part_has, unsigned *__restrict__ done, T init, int has_init,
+             T *__restrict__ out) {
+  constexpr unsigned long long TILE = 256ull * BCX_ITEMS;
+  __shared__ __align__(16) unsigned char s_raw[8 * sizeof(T)];
+  __shared__ int s_has[8];
+  __shared__ bool s_last;
+  T *s_val = reinterpret_cast<T *>(s_raw);
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const unsigned long long lo = blockIdx.x * per_block;
+  const unsigned long long hi = lo + per_block < n ? lo + per_block : n;
+  T acc = T();
+  int acc_h = 0;  // meaningful in thread 0
+  for (unsigned long long base = lo; base < hi; base += TILE) {
+    const unsigned long long t0 = base + (unsigned long long)threadIdx.x * BCX_ITEMS;
+    T v = T();
+    int h = 0;
+#pragma unroll
+    for (int k = 0; k < BCX_ITEMS; ++k)
+      if (t0 + k < hi) bcx_comb(v, h, bcx_load(a, b, t0 + k), 1);
+    v = bcx_warp_fold(v, h);
+    if (lane == 0) { s_val[warp] = v; s_has[warp] = h; }
+    __syncthreads();
+    if (warp == 0) {
+      T w = lane < 8 ? s_val[lane] : T();
+      int wh = lane < 8 ? s_has[lane] : 0;
+      w = bcx_warp_fold(w, wh);
+      if (lane == 0) bcx_comb(acc, acc_h, w, wh);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = acc;
+    part_has[blockIdx.x] = acc_h;
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last || warp != 0) return;
+  __threadfence();
+  T r = T();
+  int rh = 0;
+  if (has_init) { r = init; rh = 1; }
+  for (unsigned base = 0; base < gridDim.x; base += 32) {
+    const unsigned i = base + lane;
+    T w = T();
+    int wh = 0;
+    if (i < gridDim.x) { w = bcx_ldcg(part + i); wh = __ldcg(part_has + i); }
+    w = bcx_warp_fold(w, wh);
+    bcx_comb(r, rh, w, wh);
+  }
+  if (lane == 0 && rh) *out = r;
+}
+)BCX";
+  return src.str();
+}
+
 inline void jit_fold(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                      const std::string &load, const char *ta, const char *tb, const void *a, const void *b,
                      size_t n, const void *init, void *out, command_queue &queue) {
-  std::ostringstream src;
-  src << jit_prelude() << defs << "\n"
-      << "typedef " << t << " T;\n"
-      << "typedef " << ta << " TA;\n"
-      << "typedef " << (tb ? tb : ta) << " TB;\n"
-      << "__device__ __forceinline__ T bcx_op(const T &_1, const T &_2) { return (T)(" << op << "); }\n"
-      << "__device__ __forceinline__ T bcx_load(const TA *__restrict__ a, const TB *__restrict__ b,"
-      << " unsigned long long i) { " << load << " }\n"
-      << "struct Acc { T v; int has; };\n"
-      << "__device__ __forceinline__ Acc comb(Acc a, Acc b) {\n"
-      << "  if (!a.has) return b; if (!b.has) return a; Acc r; r.v = bcx_op(a.v, b.v); r.has = 1; return r; }\n"
-      << "__device__ Acc block_fold(Acc a) {\n"
-      << "  __shared__ T sv[256]; __shared__ int sh[256];\n"
-      << "  sv[threadIdx.x] = a.v; sh[threadIdx.x] = a.has; __syncthreads();\n"
-      << "  for (unsigned w = 1; w < blockDim.x; w <<= 1) {\n"
-      << "    if ((threadIdx.x & (2 * w - 1)) == 0 && threadIdx.x + w < blockDim.x) {\n"
-      << "      Acc x{sv[threadIdx.x], sh[threadIdx.x]}, y{sv[threadIdx.x + w], sh[threadIdx.x + w]};\n"
-      << "      Acc z = comb(x, y); sv[threadIdx.x] = z.v; sh[threadIdx.x] = z.has; }\n"
-      << "    __syncthreads(); }\n"
-      << "  Acc r{sv[0], sh[0]}; return r; }\n"
-      << "extern \"C\" __global__ void bcx_jit_reduce_partials(const TA *__restrict__ a, const TB *__restrict__ b,"
-      << " unsigned long long n, T *__restrict__ pv, int *__restrict__ ph) {\n"
-      << "  const unsigned long long per = (n + gridDim.x - 1) / gridDim.x;\n"
-      << "  const unsigned long long b0 = blockIdx.x * per, b1 = b0 + per < n ? b0 + per : n;\n"
-      << "  Acc acc; acc.has = 0; acc.v = T();\n"
-      << "  const unsigned long long chunk = (b1 > b0 ? b1 - b0 : 0) / blockDim.x + 1;\n"
-      << "  const unsigned long long t0 = b0 + threadIdx.x * chunk;\n"
-      << "  for (unsigned long long i = t0; i < t0 + chunk && i < b1; ++i) {"
-      << " Acc x; x.v = bcx_load(a, b, i); x.has = 1; acc = comb(acc, x); }\n"
-      << "  acc = block_fold(acc);\n"
-      << "  if (threadIdx.x == 0) { pv[blockIdx.x] = acc.v; ph[blockIdx.x] = acc.has; } }\n"
-      << "extern \"C\" __global__ void bcx_jit_reduce_final(const T *__restrict__ pv, const int *__restrict__ ph,"
-      << " int count, const T *__restrict__ init, T *__restrict__ out) {\n"
-      << "  if (threadIdx.x != 0) return;\n"
-      << "  Acc acc; acc.has = init != 0; acc.v = init ? *init : T();\n"
-      << "  for (int i = 0; i < count; ++i) { Acc x{pv[i], ph[i]}; acc = comb(acc, x); }\n"
-      << "  if (acc.has) *out = acc.v; }\n";
-  const std::string s = src.str();
-  // Each thread folds a contiguous run in index order and the block folds
-  // threads in order, so non-commutative (but associative) functors work.
-  const unsigned blocks = n < 4096 ? 1u : unsigned(std::min<size_t>(size_t(sm_count()) * 4, (n + 4095) / 4096));
-  void *partials = nullptr, *flags = nullptr, *dinit = nullptr;
-  check(bcx_malloc(&partials, blocks * 16 + 16));
-  check(bcx_malloc(&flags, blocks * sizeof(int)));
-  if (init) {
-    check(bcx_malloc(&dinit, 16));
-    check(bcx_memcpy_async(dinit, init, tsize, queue.get()));
-  }
+  const std::string s = jit_fold_source(defs, op, t, tsize, load, ta, tb);
+  const int items = jit_items(tsize);
+  const size_t tile = size_t(256) * size_t(items);
+  const size_t tiles = (n + tile - 1) / tile;
+  size_t blocks = tiles < 1 ? 1 : tiles;
+  const size_t cap = size_t(sm_count()) * 4;
+  if (blocks > cap) blocks = cap;
+  const size_t tiles_per_block = (tiles + blocks - 1) / blocks;
+  blocks = tiles ? (tiles + tiles_per_block - 1) / tiles_per_block : 1;
+  unsigned long long per_block = (unsigned long long)(tiles_per_block * tile);
+  // partials, their flags and the ticket of the last block, in one temporary
+  const size_t part_bytes = (blocks * tsize + 255) & ~size_t(255);
+  const size_t has_bytes = (blocks * sizeof(int) + 255) & ~size_t(255);
+  void *tmp = nullptr;
+  check(bcx_malloc_async(&tmp, part_bytes + has_bytes + 256, queue.get()));
+  char *base = static_cast<char *>(tmp);
+  void *part = base, *part_has = base + part_bytes, *done = base + part_bytes + has_bytes;
+  check(bcx_memset_async(done, 0, 4, queue.get()));
+  std::vector<unsigned char> init_bytes(tsize + 16, 0);
+  if (init) std::memcpy(init_bytes.data(), init, tsize);
+  int has_init = init != nullptr;
   unsigned long long nn = n;
   const void *bb = b ? b : a;
-  void *a1[] = {(void *)&a, (void *)&bb, (void *)&nn, (void *)&partials, (void *)&flags};
-  jit_launch(s, "bcx_jit_reduce_partials", blocks, 256, queue, a1);
-  int count = int(blocks);
-  void *a2[] = {(void *)&partials, (void *)&flags, (void *)&count, (void *)&dinit, (void *)&out};
-  jit_launch(s, "bcx_jit_reduce_final", 1, 32, queue, a2);
-  queue.finish();
-  bcx_free(partials);
-  bcx_free(flags);
-  if (dinit) bcx_free(dinit);
+  void *args[] = {(void *)&a, (void *)&bb, (void *)&nn, (void *)&per_block, (void *)&part, (void *)&part_has,
+                  (void *)&done, (void *)init_bytes.data(), (void *)&has_init, (void *)&out};
+  jit_launch(s, "bcx_jit_fold", unsigned(blocks), 256, queue, args);
+  check(bcx_free_async(tmp, queue.get()));
+}
+
+// accumulate(first, last, init, f) where the result type T (init's type)
+// differs from the element type IT: the reference folds serially on one
+// work-item, converting every intermediate result to T (detail/
+// serial_accumulate.hpp:33-49, accumulate.hpp:31-55), so the result depends
+// on the order and cannot be reassociated.  One warp reads 32 elements at a
+// time (coalesced) and folds them in order: acc = (T)(OP) with _1 = acc,
+// _2 = the element.  Writes the result to `out` (device).
+inline std::string jit_serial_fold_source(const std::string &defs, const std::string &op, const char *t,
+                                          const char *it) {
+  std::ostringstream src;
+  src << jit_prelude() << defs << "\n"
+      << "typedef " << t << " T;\ntypedef " << it << " IT;\n"
+      << R"BCX(
+extern "C" __global__ void __launch_bounds__(32)
+bcx_jit_serial_fold(const IT *__restrict__ in, unsigned long long n, T init, T *__restrict__ out) {
+  const unsigned lane = threadIdx.x;
+  constexpr int W = (int)((sizeof(IT) + 3) / 4);
+  T acc = init;
+  for (unsigned long long b = 0; b < n; b += 32) {
+    IT v = IT();
+    if (b + lane < n) v = in[b + lane];
+    unsigned w[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) w[k] = 0u;
+    {
+      const unsigned char *src = reinterpret_cast<const unsigned char *>(&v);
+      unsigned char *dst = reinterpret_cast<unsigned char *>(w);
+      for (int k = 0; k < (int)sizeof(IT); ++k) dst[k] = src[k];
+    }
+    const unsigned cnt = (n - b) < 32ull ? (unsigned)(n - b) : 32u;
+    for (unsigned j = 0; j < cnt; ++j) {
+      unsigned x[W];
+#pragma unroll
+      for (int k = 0; k < W; ++k) x[k] = __shfl_sync(0xffffffffu, w[k], (int)j);
+      IT _2;
+      {
+        const unsigned char *src = reinterpret_cast<const unsigned char *>(x);
+        unsigned char *dst = reinterpret_cast<unsigned char *>(&_2);
+        for (int k = 0; k < (int)sizeof(IT); ++k) dst[k] = src[k];
+      }
+      const T _1 = acc;
+      acc = (T)()BCX" << op << R"BCX();
+    }
+  }
+  if (lane == 0) *out = acc;
+}
+)BCX";
+  return src.str();
+}
+
+inline void jit_serial_fold(const std::string &defs, const std::string &op, const char *t, size_t tsize,
+                            const char *it, const void *in, size_t n, const void *init, void *out,
+                            command_queue &queue) {
+  std::vector<unsigned char> init_bytes(tsize + 16, 0);
+  std::memcpy(init_bytes.data(), init, tsize);
+  unsigned long long nn = n;
+  void *args[] = {(void *)&in, (void *)&nn, (void *)init_bytes.data(), (void *)&out};
+  jit_launch(jit_serial_fold_source(defs, op, t, it), "bcx_jit_serial_fold", 1, 32, queue, args);
 }
 
 inline void jit_reduce(const std::string &defs, const std::string &op, const char *t, size_t tsize,
@@ -224,69 +449,248 @@ inline void jit_reduce(const std::string &defs, const std::string &op, const cha
   jit_fold(defs, op, t, tsize, "return a[i];", t, nullptr, in, nullptr, n, init, out, queue);
 }
 
-// Scan with a user functor: tile totals -> one block scans them -> tiles
-// rescanned from their carry.  Exclusive scans start from init.
+// Scan with a user functor: one launch of a single-pass decoupled look-back
+// scan (the design of the library's built-in scan, detail/scan_on_gpu.hpp
+// replaced): each block takes the next tile from a ticket, scans its 256 x
+// ITEMS elements in registers (a thread's run, then the warp, then the
+// block), publishes the tile's aggregate, and warp 0 looks back over 32
+// predecessor tiles per step -- bounded waits, reported through the library's
+// error word -- for the exclusive prefix, which every thread folds into its
+// outputs.  Exclusive scans start from init (tile 0 publishes init OP its
+// aggregate).  In place is allowed: every thread reads all of its elements
+// before it writes any.  Asynchronous on the queue: no host waits, and the
+// status array is a stream-ordered temporary.
+inline std::string jit_scan_source(const std::string &defs, const std::string &op, const char *t, size_t tsize) {
+  const int items = jit_items(tsize);
+  const bool packed = tsize <= 4;
+  std::ostringstream src;
+  src << jit_common(defs, op, t) << "#define BCX_ITEMS " << items << "\n#define BCX_PACKED " << (packed ? 1 : 0)
+      << R"BCX(
+#define BCX_SPIN_LIMIT (1u << 22)
+// Tile status: flag 0 = nothing yet, 1 = aggregate, 2 = inclusive prefix.
+#if BCX_PACKED
+// flag and value (<= 4 bytes) in one 64-bit word: one relaxed access each way
+__device__ __forceinline__ void bcx_publish(unsigned long long *words, unsigned *, T *, T *, unsigned long long t,
+                                            unsigned flag, const T &v) {
+  unsigned bits = 0u;
+  bcx_copy<sizeof(T)>(&bits, &v);
+  const unsigned long long x = ((unsigned long long)bits << 32) | flag;
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(words + t), "l"(x) : "memory");
+}
+__device__ __forceinline__ unsigned bcx_poll(unsigned long long *words, unsigned *, T *, T *, unsigned long long t,
+                                             T *v) {
+  unsigned long long x;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(x) : "l"(words + t) : "memory");
+  const unsigned bits = unsigned(x >> 32);
+  bcx_copy<sizeof(T)>(v, &bits);
+  return unsigned(x & 0xffffffffu);
+}
+#else
+// flag word ordered after the value by release/acquire; values read from L2
+__device__ __forceinline__ void bcx_publish(unsigned long long *, unsigned *flags, T *agg, T *inc,
+                                            unsigned long long t, unsigned flag, const T &v) {
+  (flag == 1u ? agg : inc)[t] = v;
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(flags + t), "r"(flag) : "memory");
+}
+__device__ __forceinline__ unsigned bcx_poll(unsigned long long *, unsigned *flags, T *agg, T *inc,
+                                             unsigned long long t, T *v) {
+  unsigned f;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(f) : "l"(flags + t) : "memory");
+  if (f) *v = bcx_ldcg((f == 1u ? agg : inc) + t);
+  return f;
+}
+#endif
+
+// Warp 0: exclusive prefix of tile `tile` (>= 1) over its predecessors.
+__device__ T bcx_lookback(unsigned long long *words, unsigned *flags, T *agg, T *inc, unsigned long long tile,
+                          unsigned *err) {
+  const unsigned lane = threadIdx.x & 31u;
+  T ex = T();
+  int eh = 0;
+  long long pred = (long long)tile - 1;
+  bool gave_up = false;
+  while (true) {
+    const long long t = pred - (long long)lane;
+    T v = T();
+    unsigned f = 2u;  // before tile 0: never reached (tile 0 publishes a prefix)
+    int vh = 0;
+    if (t >= 0) { f = bcx_poll(words, flags, agg, inc, (unsigned long long)t, &v); vh = 1; }
+    unsigned spins = 0;
+    while (true) {
+      const unsigned pmask = __ballot_sync(0xffffffffu, f == 2u);
+      const int first = pmask ? __ffs(pmask) - 1 : 31;
+      const unsigned need = first == 31 ? 0xffffffffu : ((2u << first) - 1u);
+      if (!(__ballot_sync(0xffffffffu, f == 0u) & need)) break;
+      if (++spins > BCX_SPIN_LIMIT) {
+        gave_up = true;
+        if (f == 0u) { f = 2u; vh = 0; }
+        break;
+      }
+      __nanosleep(spins < 32 ? 32 : 256);
+      if (f == 0u && t >= 0) f = bcx_poll(words, flags, agg, inc, (unsigned long long)t, &v);
+    }
+    const unsigned pmask = __ballot_sync(0xffffffffu, f == 2u);
+    const int first = pmask ? __ffs(pmask) - 1 : 31;
+    int wh = ((int)lane <= first) ? vh : 0;
+    // lane order is newest-first: fold from the oldest (highest lane) down
+    const T rv = bcx_shfl_idx(v, 31 - (int)lane);
+    const int rh = __shfl_sync(0xffffffffu, wh, 31 - (int)lane);
+    int fh = rh;
+    const T w = bcx_warp_fold(rv, fh);
+    if (fh) {
+      ex = eh ? bcx_op(w, ex) : w;
+      eh = 1;
+    }
+    if (pmask) break;
+    pred -= 32;
+  }
+  if (__any_sync(0xffffffffu, gave_up) && lane == 0 && err) atomicOr(err, 1u);
+  return ex;
+}
+
+template <bool FULL>
+__device__ __forceinline__ void bcx_scan_tile(const T *in, T *out, unsigned long long n, unsigned long long tile,
+                                              unsigned long long *words, unsigned *flags, T *agg, T *inc,
+                                              const T &init, int has_init, int exclusive, int vec, unsigned *err) {
+  constexpr unsigned long long TILE = 256ull * BCX_ITEMS;
+  __shared__ __align__(16) unsigned char s_raw[9 * sizeof(T)];
+  __shared__ int s_has[9];
+  T *s_val = reinterpret_cast<T *>(s_raw);  // [0, 8): warp totals; [8]: tile prefix
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const unsigned long long t0 = tile * TILE + (unsigned long long)threadIdx.x * BCX_ITEMS;
+  int cnt = BCX_ITEMS;
+  if (!FULL) {
+    const long long r = (long long)n - (long long)t0;
+    cnt = r <= 0 ? 0 : (r < BCX_ITEMS ? (int)r : BCX_ITEMS);
+  }
+  T x[BCX_ITEMS];
+  if (FULL && vec) {
+    constexpr int V = (int)(BCX_ITEMS * sizeof(T) / 16);
+    uint4 u[V > 0 ? V : 1];
+#pragma unroll
+    for (int j = 0; j < V; ++j) u[j] = __ldcs(reinterpret_cast<const uint4 *>(in + t0) + j);
+    bcx_copy<(sizeof(x) < sizeof(u) ? sizeof(x) : sizeof(u))>(x, u);
+  } else {
+#pragma unroll
+    for (int k = 0; k < BCX_ITEMS; ++k) x[k] = (FULL || k < cnt) ? in[t0 + k] : T();
+  }
+  // this thread's run, inclusive
+  T run = x[0];
+#pragma unroll
+  for (int k = 1; k < BCX_ITEMS; ++k)
+    if (FULL || k < cnt) { run = bcx_op(run, x[k]); x[k] = run; }
+  int h = FULL ? 1 : (cnt > 0);
+  // lanes of the warp, inclusive
+  T a = run;
+#pragma unroll
+  for (unsigned d = 1; d < 32; d <<= 1) {
+    const T o = bcx_shfl_up(a, d);
+    const int oh = __shfl_up_sync(0xffffffffu, h, d);
+    if (lane >= d && oh) { a = h ? bcx_op(o, a) : o; h = 1; }
+  }
+  const T lane_ex = bcx_shfl_up(a, 1);
+  int lane_eh = __shfl_up_sync(0xffffffffu, h, 1);
+  if (lane == 0) lane_eh = 0;
+  if (lane == 31) { s_val[warp] = a; s_has[warp] = h; }
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < 8 ? s_val[lane] : T();
+    int wh = lane < 8 ? s_has[lane] : 0;
+    const T agg_t = bcx_warp_fold(w, wh);
+    T ex = T();
+    int eh = 0;
+    if (tile == 0) {
+      if (has_init) { ex = init; eh = 1; }
+      const T inc_t = eh ? bcx_op(ex, agg_t) : agg_t;
+      if (lane == 0) bcx_publish(words, flags, agg, inc, 0, 2u, inc_t);
+    } else {
+      if (lane == 0) bcx_publish(words, flags, agg, inc, tile, 1u, agg_t);
+      ex = bcx_lookback(words, flags, agg, inc, tile, err);
+      eh = 1;
+      if (lane == 0) bcx_publish(words, flags, agg, inc, tile, 2u, bcx_op(ex, agg_t));
+    }
+    if (lane == 0) { s_val[8] = ex; s_has[8] = eh; }
+  }
+  __syncthreads();
+  // prefix of this thread's run: tile prefix, earlier warps, earlier lanes
+  T p = s_val[8];
+  int ph = s_has[8];
+  for (unsigned j = 0; j < warp; ++j) bcx_comb(p, ph, s_val[j], s_has[j]);
+  bcx_comb(p, ph, lane_ex, lane_eh);
+  T y[BCX_ITEMS];
+  if (exclusive) {
+    y[0] = ph ? p : T();
+#pragma unroll
+    for (int k = 1; k < BCX_ITEMS; ++k) y[k] = ph ? bcx_op(p, x[k - 1]) : x[k - 1];
+  } else {
+#pragma unroll
+    for (int k = 0; k < BCX_ITEMS; ++k) y[k] = ph ? bcx_op(p, x[k]) : x[k];
+  }
+  if (FULL && vec) {
+    constexpr int V = (int)(BCX_ITEMS * sizeof(T) / 16);
+    uint4 u[V > 0 ? V : 1];
+    bcx_copy<(sizeof(y) < sizeof(u) ? sizeof(y) : sizeof(u))>(u, y);
+#pragma unroll
+    for (int j = 0; j < V; ++j) __stcs(reinterpret_cast<uint4 *>(out + t0) + j, u[j]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < BCX_ITEMS; ++k)
+      if (FULL || k < cnt) out[t0 + k] = y[k];
+  }
+}
+
+extern "C" __global__ void __launch_bounds__(256)
+bcx_jit_scan(const T *in, T *out, unsigned long long n, unsigned *ticket, unsigned long long *words,
+             unsigned *flags, T *agg, T *inc, T init, int has_init, int exclusive, int vec, unsigned *err) {
+  __shared__ unsigned s_tile;
+  if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const unsigned long long tile = s_tile;
+  if (n - tile * (256ull * BCX_ITEMS) >= 256ull * BCX_ITEMS)
+    bcx_scan_tile<true>(in, out, n, tile, words, flags, agg, inc, init, has_init, exclusive, vec, err);
+  else
+    bcx_scan_tile<false>(in, out, n, tile, words, flags, agg, inc, init, has_init, exclusive, vec, err);
+}
+)BCX";
+  return src.str();
+}
+
 inline void jit_scan(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                      const void *in, void *out, size_t n, bool exclusive, const void *init,
                      command_queue &queue) {
   if (n == 0) return;
-  const unsigned kTile = 1024;
-  std::ostringstream src;
-  src << jit_prelude() << defs << "\n"
-      << "typedef " << t << " T;\n"
-      << "__device__ __forceinline__ T bcx_op(const T &_1, const T &_2) { return (T)(" << op << "); }\n"
-      << "extern \"C\" __global__ void bcx_jit_scan_tiles(const T *__restrict__ in, unsigned long long n, T *__restrict__ sums) {\n"
-      << "  const unsigned long long b0 = (unsigned long long)blockIdx.x * " << kTile << ";\n"
-      << "  if (threadIdx.x == 0) { T acc = in[b0]; for (unsigned long long i = b0 + 1; i < b0 + " << kTile
-      << " && i < n; ++i) acc = bcx_op(acc, in[i]); sums[blockIdx.x] = acc; } }\n"
-      << "extern \"C\" __global__ void bcx_jit_scan_sums(T *__restrict__ sums, unsigned tiles, const T *__restrict__ init, int has_init) {\n"
-      << "  if (threadIdx.x != 0) return;\n"
-      << "  T run = has_init ? *init : sums[0]; int started = has_init;\n"
-      << "  for (unsigned i = 0; i < tiles; ++i) { T s = sums[i];\n"
-      << "    if (!started) { sums[i] = T(); run = s; started = 1; continue; }\n"
-      << "    sums[i] = run; run = bcx_op(run, s); } }\n"
-      << "extern \"C\" __global__ void bcx_jit_scan_apply(const T *__restrict__ in, T *__restrict__ out, unsigned long long n,"
-      << " const T *__restrict__ sums, int exclusive, int has_carry) {\n"
-      << "  __shared__ T buf[" << kTile << "];\n"
-      << "  const unsigned long long b0 = (unsigned long long)blockIdx.x * " << kTile << ";\n"
-      << "  const unsigned cnt = (unsigned)((n - b0) < " << kTile << " ? (n - b0) : " << kTile << ");\n"
-      << "  for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) buf[i] = in[b0 + i];\n"
-      << "  __syncthreads();\n"
-      << "  if (threadIdx.x == 0) {\n"
-      << "    const bool carry = has_carry || blockIdx.x > 0;\n"
-      << "    T run = carry ? sums[blockIdx.x] : T();\n"
-      << "    for (unsigned i = 0; i < cnt; ++i) { T x = buf[i];\n"
-      << "      if (exclusive) { buf[i] = run; run = (carry || i > 0) ? bcx_op(run, x) : x; }\n"
-      << "      else { run = (carry || i > 0) ? bcx_op(run, x) : x; buf[i] = run; } } }\n"
-      << "  __syncthreads();\n"
-      << "  for (unsigned i = threadIdx.x; i < cnt; i += blockDim.x) out[b0 + i] = buf[i]; }\n";
-  const std::string s = src.str();
-  const unsigned tiles = unsigned((n + kTile - 1) / kTile);
-  void *sums = nullptr, *dinit = nullptr, *tmp = nullptr;
-  check(bcx_malloc(&sums, size_t(tiles) * tsize + 16));
-  if (exclusive && init) {
-    check(bcx_malloc(&dinit, 16));
-    check(bcx_memcpy_async(dinit, init, tsize, queue.get()));
-  }
-  const void *src_in = in;
-  if (in == out) {  // in place: scan from a copy
-    check(bcx_malloc(&tmp, n * tsize));
-    check(bcx_memcpy_async(tmp, in, n * tsize, queue.get()));
-    src_in = tmp;
-  }
-  unsigned long long nn = n;
-  void *a1[] = {(void *)&src_in, (void *)&nn, (void *)&sums};
-  jit_launch(s, "bcx_jit_scan_tiles", tiles, 32, queue, a1);
-  int has_init = dinit != nullptr;
-  void *a2[] = {(void *)&sums, (void *)&tiles, (void *)&dinit, (void *)&has_init};
-  jit_launch(s, "bcx_jit_scan_sums", 1, 32, queue, a2);
+  const std::string s = jit_scan_source(defs, op, t, tsize);
+  const int items = jit_items(tsize);
+  const bool packed = tsize <= 4;
+  const size_t tile = size_t(256) * size_t(items);
+  const size_t tiles = (n + tile - 1) / tile;
+  // ticket | status words (packed) or flags + aggregates + inclusive prefixes
+  const size_t a256 = 255;
+  const size_t flag_bytes = packed ? ((tiles * 8 + a256) & ~a256) : ((tiles * 4 + a256) & ~a256);
+  const size_t val_bytes = packed ? 0 : ((tiles * tsize + a256) & ~a256);
+  void *tmp = nullptr;
+  check(bcx_malloc_async(&tmp, 256 + flag_bytes + 2 * val_bytes, queue.get()));
+  char *base = static_cast<char *>(tmp);
+  void *ticket = base;
+  void *words = packed ? base + 256 : nullptr;
+  void *flags = packed ? nullptr : base + 256;
+  void *agg = packed ? nullptr : base + 256 + flag_bytes;
+  void *inc = packed ? nullptr : base + 256 + flag_bytes + val_bytes;
+  check(bcx_memset_async(tmp, 0, 256 + flag_bytes, queue.get()));
+  void *err = nullptr;
+  check(bcx_device_error_word(&err));
+  std::vector<unsigned char> init_bytes(tsize + 16, 0);
+  int has_init = exclusive && init != nullptr;
+  if (has_init) std::memcpy(init_bytes.data(), init, tsize);
   int ex = exclusive ? 1 : 0;
-  void *a3[] = {(void *)&src_in, (void *)&out, (void *)&nn, (void *)&sums, (void *)&ex, (void *)&has_init};
-  jit_launch(s, "bcx_jit_scan_apply", tiles, 128, queue, a3);
-  queue.finish();
-  bcx_free(sums);
-  if (dinit) bcx_free(dinit);
-  if (tmp) bcx_free(tmp);
+  int vec = (items * tsize) % 16 == 0 && reinterpret_cast<uintptr_t>(in) % 16 == 0 &&
+            reinterpret_cast<uintptr_t>(out) % 16 == 0;
+  unsigned long long nn = n;
+  void *args[] = {(void *)&in, (void *)&out, (void *)&nn, (void *)&ticket, (void *)&words, (void *)&flags,
+                  (void *)&agg, (void *)&inc, (void *)init_bytes.data(), (void *)&has_init, (void *)&ex,
+                  (void *)&vec, (void *)&err};
+  jit_launch(s, "bcx_jit_scan", unsigned(tiles), 256, queue, args);
+  check(bcx_free_async(tmp, queue.get()));
 }
 
 }  // namespace detail
