@@ -6,8 +6,11 @@
 // reduce.hpp:225).  This server accepts requests from any thread while
 // earlier ones are on the GPU:
 //   * a scheduler thread admits requests in arrival order whenever a slot
-//     (a CUDA stream) is free and the device-memory budget covers the
-//     request's buffers and temporaries;
+//     (a CUDA stream) is free, the device's free memory (measured at each
+//     admission: the driver's free bytes plus what the stream-ordered pool
+//     holds unused) covers the request's buffers and temporaries, and so does
+//     the server's budget; a request that cannot fit while nothing else runs
+//     fails with BCX_MEM_ALLOCATION_FAILURE;
 //   * small requests that wait together with the same (kind, dtype, value
 //     size) are packed into one batch and run as ONE segmented launch
 //     (bcx_segmented_sort_pairs / bcx_segmented_scan / bcx_segmented_reduce);
@@ -91,6 +94,11 @@ struct bcx_server {
   bool stop = false;
   std::thread scheduler;
   int device = 0;
+  // Fault injection for tests (bcx_server_inject_faults): a fixed figure for
+  // the device's free memory instead of the measured one (0 = measure), and a
+  // number of batch allocations to fail.
+  size_t fake_free = 0;
+  int fail_allocs = 0;
   // statistics
   uint64_t completed = 0, batches = 0, batched_requests = 0;
   std::vector<double> latencies_ms;
@@ -339,6 +347,28 @@ size_t batch_temp(const std::vector<std::shared_ptr<Request>> &reqs, size_t n) {
   return rc ? 0 : tb;
 }
 
+// Device memory a new batch can still get: the driver's free memory plus what
+// the stream-ordered pool holds unused (freed batches stay cached there).
+size_t available_memory(const bcx_server *srv) {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, srv->device) == cudaSuccess) {
+    uint64_t reserved = 0, used = 0;
+    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+      free_b += size_t(reserved - used);
+  }
+  return free_b;
+}
+
+// Takes one injected allocation failure, if any are left (server lock held).
+bool take_injected_failure(bcx_server *srv) {
+  if (srv->fail_allocs <= 0) return false;
+  --srv->fail_allocs;
+  return true;
+}
+
 // No request waiting or running (server lock held).
 bool idle_locked(const bcx_server *srv) {
   if (!srv->pending.empty()) return false;
@@ -391,6 +421,7 @@ void scheduler_loop(bcx_server *srv) {
         n += q->r.n;
       }
     }
+    const size_t fake = srv->fake_free;
     lk.unlock();
     const size_t temp = batch_temp(reqs, n);
     size_t bytes = 0;
@@ -403,10 +434,28 @@ void scheduler_loop(bcx_server *srv) {
       const size_t pieces = 4 * reqs.size() + 2 * bytes / kCopyChunkBytes;
       bytes += temp + 3 * 256 + align256((reqs.size() + 1) * 8) + pieces * sizeof(CopyChunk);
     }
+    // Admission by free device memory, measured now (outside the lock), and by
+    // the server's budget.
+    const size_t avail = fake ? fake : available_memory(srv);
     lk.lock();
-    if (srv->used + bytes > srv->budget && srv->used > 0) {
+    const bool fits = srv->used + bytes <= srv->budget && bytes <= avail;
+    if (!fits && srv->used > 0) {
       // Not enough memory right now: wait for a completion to free some.
       srv->cv.wait(lk);
+      continue;
+    }
+    if (!fits && bytes > avail) {
+      // Nothing of ours is running and the device still lacks the memory:
+      // fail the batch's requests instead of waiting for memory that only
+      // another process could free.
+      for (auto &r : reqs) {
+        auto it = std::find(srv->pending.begin(), srv->pending.end(), r);
+        if (it != srv->pending.end()) srv->pending.erase(it);
+        r->status = BCX_MEM_ALLOCATION_FAILURE;
+        r->finished = Clock::now();
+        r->done.store(1);
+      }
+      srv->cv.notify_all();
       continue;
     }
     // Admit: remove from pending (preserving the order of the rest).
@@ -423,9 +472,16 @@ void scheduler_loop(bcx_server *srv) {
     srv->used += bytes;
     srv->batches += 1;
     if (reqs.size() > 1) srv->batched_requests += reqs.size();
+    const bool inject = take_injected_failure(srv);
     lk.unlock();
     // On success the batch belongs to its completion callback from here on.
-    const bcx_status rc = launch_batch(srv, b, temp);
+    bcx_status rc = BCX_SUCCESS;
+    if (inject) {
+      set_error("server: injected allocation failure");
+      rc = BCX_MEM_ALLOCATION_FAILURE;
+    } else {
+      rc = launch_batch(srv, b, temp);
+    }
     if (rc && b->dev) cudaFreeAsync(b->dev, srv->slots[slot].stream);
     lk.lock();
     if (rc) {
@@ -473,6 +529,18 @@ bcx_status bcx_server_configure(bcx_server *srv, size_t small_limit, size_t batc
   srv->small_limit = small_limit;
   if (batch_elems) srv->batch_elems = batch_elems;
   if (batch_count) srv->batch_count = batch_count;
+  return BCX_SUCCESS;
+}
+
+bcx_status bcx_server_inject_faults(bcx_server *srv, size_t fake_free_bytes, int fail_allocations) {
+  BCX_CHECK(srv, BCX_INVALID_VALUE, "NULL server");
+  BCX_CHECK(fail_allocations >= 0, BCX_INVALID_VALUE, "fail_allocations must be >= 0");
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->fake_free = fake_free_bytes;
+    srv->fail_allocs = fail_allocations;
+  }
+  srv->cv.notify_all();
   return BCX_SUCCESS;
 }
 

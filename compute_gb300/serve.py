@@ -64,6 +64,13 @@ class Server:
         check(rc, "server_wait")
         return ms.value
 
+    def inject_faults(self, fake_free_bytes: int = 0, fail_allocations: int = 0) -> None:
+        """Test hook: admission sees `fake_free_bytes` of free device memory (0 =
+        the measured figure); the next `fail_allocations` batches fail as if
+        their device allocation had failed."""
+        check(lib().bcx_server_inject_faults(self._h, int(fake_free_bytes), int(fail_allocations)),
+              "server_inject_faults")
+
     def drain(self) -> None:
         check(lib().bcx_server_drain(self._h), "server_drain")
 

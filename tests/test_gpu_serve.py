@@ -105,3 +105,59 @@ def test_server_device_resident_out_of_place(cuda, small_limit):
     assert np.array_equal(os_.cpu().numpy().view(np.uint32), oracle.scan(shared, "uint", exclusive=True))
     as_u64 = shared.view(np.uint64)  # the same bytes read as n/2 uint64 values
     assert int(red.cpu().numpy().view(np.uint64)[0]) == int(oracle.fold(as_u64, "ulong"))
+
+
+def _sort_request(srv, rng, n):
+    keys = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
+    k = keys.copy()
+    v = np.arange(n, dtype=np.uint32)
+    return keys, k, v, srv.submit("sort_by_key", "uint", k, values=v)
+
+
+def test_server_admission_by_free_memory(cuda):
+    """Admission follows the device's free memory: with free memory faked below
+    what a request needs and nothing else running, the request fails with
+    BCX_MEM_ALLOCATION_FAILURE instead of waiting forever; a request that fits
+    is served; with the real figure back, the large request is served too."""
+    from compute_gb300 import BcxError
+    from compute_gb300._lib import MEM_ALLOCATION_FAILURE
+    from compute_gb300.serve import Server
+    rng = np.random.default_rng(11)
+    with Server(slots=2) as srv:
+        srv.inject_faults(fake_free_bytes=64 << 10)  # 64 KiB "free"
+        _, _, _, t_big = _sort_request(srv, rng, 1 << 20)  # needs about 8 MiB
+        with pytest.raises(BcxError) as e:
+            srv.wait(t_big, timeout=60)
+        assert e.value.status == MEM_ALLOCATION_FAILURE
+        keys, k, v, t_small = _sort_request(srv, rng, 1000)  # about 8 KB: fits
+        srv.wait(t_small, timeout=60)
+        rk, rv = oracle.radix_sort(keys, "uint", values=np.arange(1000, dtype=np.uint32))
+        assert np.array_equal(k, rk) and np.array_equal(v, rv)
+        srv.inject_faults(fake_free_bytes=0)
+        keys, k, v, t = _sort_request(srv, rng, 1 << 20)
+        srv.wait(t, timeout=60)
+        rk, rv = oracle.radix_sort(keys, "uint", values=np.arange(1 << 20, dtype=np.uint32))
+        assert np.array_equal(k, rk) and np.array_equal(v, rv)
+
+
+def test_server_survives_allocation_failure(cuda):
+    """A batch whose device allocation fails ends its requests with
+    BCX_MEM_ALLOCATION_FAILURE; the server goes on serving later requests
+    correctly and keeps its memory accounting balanced."""
+    from compute_gb300 import BcxError
+    from compute_gb300._lib import MEM_ALLOCATION_FAILURE
+    from compute_gb300.serve import Server
+    rng = np.random.default_rng(12)
+    with Server(slots=2) as srv:
+        srv.inject_faults(fail_allocations=1)
+        _, _, _, t1 = _sort_request(srv, rng, 5000)
+        with pytest.raises(BcxError) as e:
+            srv.wait(t1, timeout=60)
+        assert e.value.status == MEM_ALLOCATION_FAILURE
+        outs = [_sort_request(srv, rng, n) for n in (5000, 70_000, 300_001)]
+        for keys, k, v, t in outs:
+            srv.wait(t, timeout=60)
+            rk, rv = oracle.radix_sort(keys, "uint", values=np.arange(keys.size, dtype=np.uint32))
+            assert np.array_equal(k, rk) and np.array_equal(v, rv)
+        srv.drain()
+        assert srv.stats()["used_bytes"] == 0
