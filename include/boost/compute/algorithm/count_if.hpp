@@ -13,6 +13,7 @@
 #include <string>
 
 #include <boost/compute/algorithm/transform_reduce.hpp>
+#include <boost/compute/types/tuple.hpp>
 
 namespace boost {
 namespace compute {
@@ -26,7 +27,7 @@ inline size_t count_where(InputIterator first, InputIterator last, const std::st
   if (first == last) return 0;
   device_range<InputIterator> in(first, last, queue);
   vector<ulong_> out(1, queue.get_context());
-  jit_fold(defs, "_1 + _2", "unsigned long long", sizeof(unsigned long long),
+  jit_fold(type_definition<A>::get() + defs, "_1 + _2", "unsigned long long", sizeof(unsigned long long),
            "const auto _1 = a[i]; return (T)((" + pred + ") ? 1ull : 0ull);", cuda_type_name<A>::get(), nullptr,
            in.ptr, nullptr, in.n, nullptr, out.data(), queue);
   return size_t(out.begin().read(queue));

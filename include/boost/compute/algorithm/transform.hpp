@@ -13,6 +13,7 @@
 #include <boost/compute/detail/device_range.hpp>
 #include <boost/compute/functional.hpp>
 #include <boost/compute/iterator/transform_iterator.hpp>
+#include <boost/compute/types/tuple.hpp>
 
 namespace boost {
 namespace compute {
@@ -47,8 +48,9 @@ transform(InputIterator first, InputIterator last, buffer_iterator<T> result, F 
           command_queue &queue = system::default_queue()) {
   typedef typename std::iterator_traits<InputIterator>::value_type A;
   detail::device_range<InputIterator> in(first, last, queue);
-  detail::jit_transform(f.defs(), f.print(), detail::cuda_type_name<A>::get(), "", detail::cuda_type_name<T>::get(),
-                        sizeof(A), 0, sizeof(T), in.ptr, nullptr, result.get_ptr(), in.n, queue);
+  detail::jit_transform(detail::type_definition<A>::get() + detail::type_definition<T>::get() + f.defs(), f.print(),
+                        detail::cuda_type_name<A>::get(), "", detail::cuda_type_name<T>::get(), sizeof(A), 0,
+                        sizeof(T), in.ptr, nullptr, result.get_ptr(), in.n, queue);
   if (!std::is_same<InputIterator, buffer_iterator<A> >::value) queue.finish();
   return result + std::ptrdiff_t(in.n);
 }
@@ -61,7 +63,9 @@ transform(InputIterator1 first1, InputIterator1 last1, InputIterator2 first2, bu
   typedef typename std::iterator_traits<InputIterator2>::value_type B;
   detail::device_range<InputIterator1> a(first1, last1, queue);
   detail::device_range<InputIterator2> b(first2, first2 + std::ptrdiff_t(a.n), queue);
-  detail::jit_transform(f.defs(), f.print(), detail::cuda_type_name<A>::get(), detail::cuda_type_name<B>::get(),
+  detail::jit_transform(detail::type_definition<A>::get() + detail::type_definition<B>::get() +
+                            detail::type_definition<T>::get() + f.defs(),
+                        f.print(), detail::cuda_type_name<A>::get(), detail::cuda_type_name<B>::get(),
                         detail::cuda_type_name<T>::get(), sizeof(A), sizeof(B), sizeof(T), a.ptr, b.ptr,
                         result.get_ptr(), a.n, queue);
   queue.finish();

@@ -9,6 +9,7 @@
 #ifndef BOOST_COMPUTE_LAMBDA_HPP
 #define BOOST_COMPUTE_LAMBDA_HPP
 
+#include <cstddef>
 #include <string>
 #include <type_traits>
 
@@ -129,6 +130,20 @@ template <class A, class = typename std::enable_if<is_node<A>::value>::type>
 unary_node<A> operator-(const A &a) { return unary_node<A>(a, "-"); }
 template <class A, class = typename std::enable_if<is_node<A>::value>::type>
 unary_node<A> operator!(const A &a) { return unary_node<A>(a, "!"); }
+
+// get<N>(expr): element N of a tuple, component N of a vector type
+// (lambda/get.hpp of the reference).
+template <std::size_t N, class A>
+struct get_node : expr_base<get_node<N, A> > {
+  A a;
+  explicit get_node(const A &a_) : a(a_) {}
+  std::string print() const { return "bcx_get<" + std::to_string(N) + ">(" + a.print() + ")"; }
+  std::string defs() const { return a.defs(); }
+};
+template <std::size_t N, class A, class = typename std::enable_if<is_node<A>::value>::type>
+get_node<N, A> get(const A &a) {
+  return get_node<N, A>(a);
+}
 
 #define BOOST_COMPUTE_LAMBDA_FN1(NAME, TEXT)                                    \
   template <class A, class = typename std::enable_if<is_node<A>::value>::type>  \

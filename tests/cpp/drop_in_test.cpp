@@ -12,6 +12,9 @@
 #include <vector>
 
 #include <boost/compute.hpp>
+#include <boost/compute/container/mapped_view.hpp>
+#include <boost/compute/iterator/zip_iterator.hpp>
+#include <tuple>
 
 namespace compute = boost::compute;
 
@@ -248,6 +251,165 @@ static void jit_cases(compute::command_queue &q) {
     threw = !e.build_log().empty();
   }
   CHECK(threw);
+}
+
+// User functors on the generated single-pass scan and one-launch fold, at
+// sizes with many tiles (look-back across tiles, in-order folds across blocks).
+static void jit_large_cases(compute::command_queue &q) {
+  // test/test_scan.cpp:414-436 (exclusive multiplies, init 10, 1000 twos) with
+  // the functor given as a user function instead of multiplies<int>
+  BOOST_COMPUTE_FUNCTION(int, times, (int x, int y), { return x * y; });
+  compute::vector<int> tw(1000, 2, q);
+  compute::exclusive_scan(tw.begin(), tw.end(), tw.begin(), 10, times, q);
+  std::vector<int> expect_tw(1000, 2);
+  expect_tw[0] = 10;
+  {
+    unsigned run = 1;
+    for (size_t i = 0; i < expect_tw.size(); ++i) {
+      run *= unsigned(expect_tw[i]);
+      expect_tw[i] = int(run);
+    }
+  }
+  CHECK(to_host(tw, q) == expect_tw);
+  // inclusive plus through a user function over 3,000,017 elements (wraps)
+  const size_t n = 3000017;
+  std::vector<int> h(n);
+  for (size_t i = 0; i < n; ++i) h[i] = int(i % 1000) - 500 + int((i * 2654435761u) >> 28);
+  BOOST_COMPUTE_FUNCTION(int, add_u, (int a, int b), { return (int)((unsigned)a + (unsigned)b); });
+  compute::vector<int> dv(h.begin(), h.end(), q), dout(n, q.get_context());
+  compute::inclusive_scan(dv.begin(), dv.end(), dout.begin(), add_u, q);
+  std::vector<int> ref(n);
+  {
+    unsigned run = 0;
+    for (size_t i = 0; i < n; ++i) {
+      run += unsigned(h[i]);
+      ref[i] = int(run);
+    }
+  }
+  CHECK(to_host(dout, q) == ref);
+  // exclusive, init 7, in place
+  compute::exclusive_scan(dv.begin(), dv.end(), dv.begin(), 7, add_u, q);
+  {
+    unsigned run = 7;
+    for (size_t i = 0; i < n; ++i) {
+      const unsigned x = unsigned(h[i]);
+      ref[i] = int(run);
+      run += x;
+    }
+  }
+  CHECK(to_host(dv, q) == ref);
+  // a non-commutative associative functor on a 16-byte type: products of
+  // 2x2 integer matrices mod 2^32, scanned and folded in input order
+  BOOST_COMPUTE_FUNCTION(compute::int4_, matmul, (compute::int4_ a, compute::int4_ b), {
+    const unsigned a0 = a.x, a1 = a.y, a2 = a.z, a3 = a.w, b0 = b.x, b1 = b.y, b2 = b.z, b3 = b.w;
+    return make_int4((int)(a0 * b0 + a1 * b2), (int)(a0 * b1 + a1 * b3), (int)(a2 * b0 + a3 * b2),
+                     (int)(a2 * b1 + a3 * b3));
+  });
+  const size_t m = 1000003;
+  std::vector<compute::int4_> hm(m);
+  std::mt19937 gen(7);
+  for (size_t i = 0; i < m; ++i)
+    hm[i] = compute::int4_(int(gen() % 4) - 1, int(gen() % 4) - 1, int(gen() % 4) - 1, int(gen() % 4) - 1);
+  auto mul = [](const compute::int4_ &a, const compute::int4_ &b) {
+    const unsigned a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3], b0 = b[0], b1 = b[1], b2 = b[2], b3 = b[3];
+    return compute::int4_(int(a0 * b0 + a1 * b2), int(a0 * b1 + a1 * b3), int(a2 * b0 + a3 * b2),
+                          int(a2 * b1 + a3 * b3));
+  };
+  compute::vector<compute::int4_> dm(hm.begin(), hm.end(), q), dmo(m, q.get_context());
+  compute::inclusive_scan(dm.begin(), dm.end(), dmo.begin(), matmul, q);
+  std::vector<compute::int4_> got = to_host(dmo, q);
+  std::vector<compute::int4_> pref(m);
+  pref[0] = hm[0];
+  for (size_t i = 1; i < m; ++i) pref[i] = mul(pref[i - 1], hm[i]);
+  CHECK(got == pref);
+  compute::vector<compute::int4_> fold(1, q.get_context());
+  compute::reduce(dm.begin(), dm.end(), fold.begin(), matmul, q);
+  CHECK(fold.begin().read(q) == pref[m - 1]);
+}
+
+// zip_iterator, mapped_view and accumulate with an init of another type.
+static void zip_view_cases(compute::command_queue &q) {
+  // test/test_zip_iterator.cpp:47-105 (distance)
+  compute::vector<char> cvec(5, q.get_context());
+  compute::vector<int> ivec(5, q.get_context());
+  CHECK(std::distance(compute::make_zip_iterator(std::make_tuple(cvec.begin(), ivec.begin())),
+                      compute::make_zip_iterator(std::make_tuple(cvec.end(), ivec.end()))) == 5);
+  // test/test_zip_iterator.cpp:107-155 (copy three vectors into a vector of tuples)
+  char cd[] = {'x', 'y', 'z'};
+  int id[] = {4, 7, 9};
+  float fd[] = {3.2f, 4.5f, 7.6f};
+  compute::vector<char> cv(cd, cd + 3, q);
+  compute::vector<int> iv(id, id + 3, q);
+  compute::vector<float> fv(fd, fd + 3, q);
+  compute::vector<std::tuple<char, int, float> > tv(3, q.get_context());
+  compute::copy(compute::make_zip_iterator(std::make_tuple(cv.begin(), iv.begin(), fv.begin())),
+                compute::make_zip_iterator(std::make_tuple(cv.end(), iv.end(), fv.end())), tv.begin(), q);
+  std::vector<std::tuple<char, int, float> > ht = to_host(tv, q);
+  CHECK(ht.size() == 3 && ht[0] == std::make_tuple('x', 4, 3.2f) && ht[1] == std::make_tuple('y', 7, 4.5f) &&
+        ht[2] == std::make_tuple('z', 9, 7.6f));
+  // test/test_zip_iterator.cpp:157-207 (transform with get<N>)
+  int d1[] = {0, 2, 4, 6, 8};
+  int d2[] = {1, 3, 5, 7, 9};
+  compute::vector<int> in1(d1, d1 + 5, q), in2(d2, d2 + 5, q), out(5, q.get_context());
+  compute::transform(compute::make_zip_iterator(std::make_tuple(in1.begin())),
+                     compute::make_zip_iterator(std::make_tuple(in1.end())), out.begin(), compute::get<0>(), q);
+  CHECK((to_host(out, q) == std::vector<int>{0, 2, 4, 6, 8}));
+  compute::transform(compute::make_zip_iterator(std::make_tuple(in2.begin(), in1.begin())),
+                     compute::make_zip_iterator(std::make_tuple(in2.end(), in1.end())), out.begin(),
+                     compute::get<1>(), q);
+  CHECK((to_host(out, q) == std::vector<int>{0, 2, 4, 6, 8}));
+  // three ranges into a user function of the tuple
+  BOOST_COMPUTE_FUNCTION(float, fma3, (std::tuple<float, float, float> t),
+                         { return boost_tuple_get(t, 0) * boost_tuple_get(t, 1) + boost_tuple_get(t, 2); });
+  float a3[] = {1.f, 2.f, 3.f}, b3[] = {4.f, 5.f, 6.f}, c3[] = {0.5f, 0.25f, 0.125f};
+  compute::vector<float> va(a3, a3 + 3, q), vb(b3, b3 + 3, q), vc(c3, c3 + 3, q), vr(3, q.get_context());
+  compute::transform(compute::make_zip_iterator(std::make_tuple(va.begin(), vb.begin(), vc.begin())),
+                     compute::make_zip_iterator(std::make_tuple(va.end(), vb.end(), vc.end())), vr.begin(), fma3, q);
+  CHECK((to_host(vr, q) == std::vector<float>{4.5f, 10.25f, 18.125f}));
+  // the lambda form, get<0>(_1) < 5, in count_if (test/test_count.cpp:182)
+  using compute::lambda::get;
+  CHECK(compute::count_if(compute::make_zip_iterator(std::make_tuple(in1.begin(), in2.begin())),
+                          compute::make_zip_iterator(std::make_tuple(in1.end(), in2.end())),
+                          get<0>(compute::_1) < 5, q) == 3);
+  // test/test_accumulate.cpp:258-299 (std::accumulate equality through a
+  // mapped_view, int init over int, float and double data)
+  std::vector<int> h1 = {1, 2, 3, 4};
+  {
+    compute::mapped_view<int> view(h1.data(), h1.size(), q.get_context());
+    CHECK(compute::accumulate(view.begin(), view.end(), 0, q) == std::accumulate(h1.begin(), h1.end(), 0));
+  }
+  h1.assign(10000, 2);
+  {
+    compute::mapped_view<int> view(h1.data(), h1.size(), q.get_context());
+    CHECK(compute::accumulate(view.begin(), view.end(), 0, q) == std::accumulate(h1.begin(), h1.end(), 0));
+  }
+  std::vector<float> h2 = {1.2f, 2.3f, 4.5f, 6.7f, 8.9f};
+  {
+    compute::mapped_view<float> view(h2.data(), h2.size(), q.get_context());
+    CHECK(compute::accumulate(view.begin(), view.end(), 0, q) == std::accumulate(h2.begin(), h2.end(), 0));
+  }
+  h2.assign(10000, 1.01f);
+  {
+    compute::mapped_view<float> view(h2.data(), h2.size(), q.get_context());
+    CHECK(compute::accumulate(view.begin(), view.end(), 0, q) == std::accumulate(h2.begin(), h2.end(), 0));
+  }
+  std::vector<double> h3(10000, 2.02);
+  {
+    compute::mapped_view<double> view(h3.data(), h3.size(), q.get_context());
+    CHECK(compute::accumulate(view.begin(), view.end(), 0, q) == std::accumulate(h3.begin(), h3.end(), 0));
+  }
+  // a device sort writing through a mapped view into host memory
+  std::vector<int> hs(100003);
+  std::mt19937 gen(3);
+  for (auto &x : hs) x = int(gen() % 1000000) - 500000;
+  std::vector<int> expect = hs;
+  std::sort(expect.begin(), expect.end());
+  {
+    compute::mapped_view<int> view(hs.data(), hs.size(), q.get_context());
+    compute::sort(view.begin(), view.end(), q);
+    view.map(q);
+  }
+  CHECK(hs == expect);
 }
 
 static void transform_reduce_cases(compute::command_queue &q) {
@@ -506,7 +668,20 @@ static void async_cases(compute::command_queue &q) {
   CHECK(never.status() == compute::event::complete);
 }
 
+static int run_all();
+
 int main() {
+  try {
+    return run_all();
+  } catch (const compute::program_build_failure &e) {
+    std::printf("FAILED: program_build_failure\n%s\n", e.build_log().c_str());
+  } catch (const std::exception &e) {
+    std::printf("FAILED: exception %s\n", e.what());
+  }
+  return 1;
+}
+
+static int run_all() {
   compute::command_queue &q = compute::system::default_queue();
   readme_example();
   sort_cases(q);
@@ -515,6 +690,8 @@ int main() {
   transform_cases(q);
   reduce_by_key_cases(q);
   jit_cases(q);
+  jit_large_cases(q);
+  zip_view_cases(q);
   transform_reduce_cases(q);
   scan_family_cases(q);
   comparator_sort_cases(q);
