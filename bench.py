@@ -56,9 +56,8 @@ WORKLOAD = ("sort_by_key uint32 keys (uniform 32-bit) with uint32 values (iota),
 SORT_BYTES_PER_PAIR = 68
 ONESWEEP_BYTES_PER_PAIR = 16
 # DRAM traffic of one onesweep launch per pair: dram__bytes_read.sum +
-# dram__bytes_write.sum of one captured launch at 2^25 pairs (502.4 MB), per
-# pair, scaled to the 2^28-pair launch by the pairs it moves
-# (profiles/radix_onesweep_u32_pairs.md).
+# dram__bytes_write.sum of one captured launch at 2^25 pairs, per pair, scaled
+# to the 2^28-pair launch by the pairs it moves.
 ONESWEEP_DRAM_BYTES_PER_PAIR = 502.352384e6 / (1 << 25)
 
 
@@ -175,6 +174,43 @@ def cpu_sort_baseline(sample=1 << 24, trials=3):
             "sample": f"{sample} uint32 pairs (uniform keys, iota values), best of {trials}, "
                       f"merge_sort_by_key_on_cpu restated in oracle/oracle.cpp",
             "median_s": statistics.median(times)}
+
+
+def cpu_prims_baseline(sample=1 << 27, trials=3):
+    """The reference's CPU-device scan (scan_on_cpu), reduce (reduce_on_cpu)
+    and the saxpy transform, as restated in the oracle, on `sample` elements
+    with every host thread: GB/s over the same algorithmic bytes as the GPU
+    lines (scan 8 B, reduce 4 B, saxpy 12 B per element)."""
+    import numpy as np
+
+    import oracle
+    threads = oracle.hardware_threads()
+    rng = np.random.default_rng(20261203)
+    a = rng.integers(0, 100, size=sample).astype(np.int32)
+    out = np.empty_like(a)
+    x = rng.uniform(-1, 1, size=sample).astype(np.float32)
+    y = rng.uniform(-1, 1, size=sample).astype(np.float32)
+    r = np.empty_like(x)
+
+    def best(fn):
+        ts = []
+        for _ in range(trials):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    out_lines = {}
+    for name, fn, bpe, ref in [
+            ("exclusive_scan_i32", lambda: oracle.cpu_exclusive_scan_i32(a, out, 0, threads=threads), 8,
+             "scan_on_cpu"),
+            ("reduce_i32", lambda: oracle.cpu_reduce_i32(a, threads=threads), 4, "reduce_on_cpu"),
+            ("saxpy_f32", lambda: oracle.cpu_saxpy_f32(2.5, x, y, r, threads=threads), 12,
+             "transform (2.5f * x + y)")]:
+        t = best(fn)
+        out_lines[name] = {"value": bpe * sample / t / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+                           "sample": f"{sample} elements, best of {trials}, {ref} restated in oracle/oracle.cpp"}
+    return out_lines
 
 
 def run_reference(args):
@@ -324,6 +360,12 @@ def main():
         psteps = 0
     if psteps:
         prims = run_primitives(torch, bc, dev, g, psteps, hbm)
+        if rank == 0:
+            torch.cuda.synchronize()
+            prims["drop_in_generated"] = run_drop_in(psteps)
+            for v in prims["drop_in_generated"].values():
+                if isinstance(v, dict) and "GB/s" in v:
+                    v["frac"] = v["GB/s"] / hbm
     precision = None
     if args.only in ("all", "precision"):
         precision = run_precision(torch, bc, dev, hbm)
@@ -338,6 +380,11 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_sort_baseline()
+        if prims:
+            for name, line in cpu_prims_baseline().items():
+                for key in prims:
+                    if key.startswith(name):
+                        prims[key]["cpu_baseline"] = line
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps,
@@ -398,6 +445,29 @@ def run_primitives(torch, bc, dev, g, psteps, hbm):
     return prims
 
 
+def run_drop_in(steps):
+    """The drop-in calls whose kernels are generated at run time (saxpy as the
+    lambda alpha * _1 + _2, user-function scans and accumulate), timed by
+    tests/cpp/drop_in_bench.cpp through the boost::compute headers."""
+    import shutil
+    import tempfile
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        return {"unavailable": "no C++ compiler"}
+    src = os.path.join(ROOT, "tests", "cpp", "drop_in_bench.cpp")
+    libdir = os.path.join(ROOT, "compute_gb300")
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = os.path.join(tmp, "drop_in_bench")
+        r = subprocess.run([cxx, "-std=c++17", "-O2", f"-I{os.path.join(ROOT, 'include')}", src, "-o", exe,
+                            f"-L{libdir}", "-lbcx", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+        if r.returncode != 0:
+            return {"unavailable": "build failed: " + r.stderr[-300:]}
+        run = subprocess.run([exe, str(steps)], capture_output=True, text=True, timeout=600)
+        if run.returncode != 0:
+            return {"failed": (run.stdout + run.stderr)[-500:]}
+        return json.loads(run.stdout.strip().splitlines()[-1])
+
+
 def run_e2e(torch, bc, rank, world):
     import numpy as np
     rng = np.random.default_rng(20261203 + rank)
@@ -420,7 +490,29 @@ def run_e2e(torch, bc, rank, world):
         per.append(time.perf_counter() - t0)
         tot += per[-1]
     tot = max_over_ranks(tot, world)
-    return {"value": job_throughput(N_SORT * e2e_steps, tot, world), "unit": "Gkeys/s",
+    # The link bound of one step: the same 2 x 4 B x n bytes copied to the
+    # device and back as plain pinned copies, no sort in between.
+    dk = torch.empty(N_SORT, dtype=torch.int32, device="cuda")
+    dv = torch.empty_like(dk)
+    copies = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dk.copy_(hk, non_blocking=True)
+        dv.copy_(hv, non_blocking=True)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        hk.copy_(dk, non_blocking=True)
+        hv.copy_(dv, non_blocking=True)
+        torch.cuda.synchronize()
+        copies.append((t1 - t0, time.perf_counter() - t1))
+    del dk, dv
+    h2d = min(c[0] for c in copies)
+    d2h = min(c[1] for c in copies)
+    link = {"h2d_ms": h2d * 1e3, "d2h_ms": d2h * 1e3, "h2d_GBps": 8 * N_SORT / h2d / 1e9,
+            "d2h_GBps": 8 * N_SORT / d2h / 1e9, "copies_ms": (h2d + d2h) * 1e3,
+            "how": "the step's 2 x 4 B x n bytes each way as plain pinned torch copies, best of 3"}
+    return {"value": job_throughput(N_SORT * e2e_steps, tot, world), "unit": "Gkeys/s", "link_bound": link,
             "h2d_bytes_per_step": 8 * N_SORT, "d2h_bytes_per_step": 8 * N_SORT,
             "ms_per_step": tot / e2e_steps * 1e3, "ms_median_step": statistics.median(per) * 1e3,
             "ms_steps": [round(x * 1e3, 2) for x in per],
