@@ -17,9 +17,10 @@
 // and per-chunk prefixes are kept; warps combine through shared memory, the
 // tile with its predecessors by decoupled look-back (order-preserving, bounded
 // waits, self-validating status words where the value allows), and a second
-// read of the tile (from L2) emits the results: run heads write the output
-// key, run ends the reduced value, and the block holding the last element
-// writes the run count -- nothing is read back to the host.  Key equality is
+// read (from L2), by only the lanes whose run holds a run head or a run end,
+// emits the results: run heads write the output key, run ends the reduced
+// value, and the block holding the last element writes the run count --
+// nothing is read back to the host.  Key equality is
 // the typed == of equal_to<T>.  Float plus with compensated=1 carries
 // Neumaier (s, c) pairs.
 #include <cuda_runtime.h>
@@ -418,27 +419,42 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   const S pre = seg_comb<P>(s_prefix, warp_excl);
   const size_t warp_end = warp_base + size_t(CH) * kWarp * N;  // first element after this warp
   const bool after_head = lane == kWarp - 1 && warp_end < n && !keys_equal(keys[warp_end], carry_key);
+  // A lane re-reads and re-folds its run of chunk j only if the run holds a
+  // run head (its key is written) or a run end (its value is written); with
+  // long runs (segment ids as keys) almost every lane skips both.  The fold
+  // order is unchanged, so results are identical.
+  constexpr uint32_t kRunMask = N >= 32 ? 0xffffffffu : ((1u << N) - 1u);
 #pragma unroll
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
-    K k[N];
-    V v[N];
-    load_run<K, N>(keys, e0, n, vec_k != 0, k);
-    load_run<V, N>(vals, e0, n, vec_v != 0, v);
     // head flag of the element after this lane's run in chunk j
     const uint32_t h_next_lane = __shfl_down_sync(0xffffffffu, heads >> (j * N), 1) & 1u;
     const uint32_t h_next_chunk = __shfl_sync(0xffffffffu, heads >> (j + 1 < CH ? (j + 1) * N : 0), 0) & 1u;
     uint32_t next_h = h_next_lane;
     if (lane == kWarp - 1) next_h = j + 1 < CH ? h_next_chunk : uint32_t(after_head);
+    const uint32_t hj = (heads >> (j * N)) & kRunMask;
+    // run ends: the next element is a head, or the element is the last one
+    uint32_t ends = (hj >> 1) | (next_h << (N - 1));
+    if (e0 >= n) {
+      ends = 0;
+    } else if (n - e0 <= size_t(N)) {
+      ends |= 1u << (n - e0 - 1);
+      ends &= n - e0 >= 32 ? 0xffffffffu : ((1u << (n - e0)) - 1u);
+    }
+    if (((hj & (keys_out ? kRunMask : 0u)) | ends) == 0) continue;
+    K k[N];
+    V v[N];
+    load_run<K, N>(keys, e0, n, vec_k != 0, k);
+    load_run<V, N>(vals, e0, n, vec_v != 0, v);
     S acc = seg_comb<P>(pre, lane_pre[j]);
 #pragma unroll
     for (int m = 0; m < N; ++m) {
       const size_t idx = e0 + m;
-      const bool h = (heads >> (j * N + m)) & 1u;
+      const bool h = (hj >> m) & 1u;
       if (idx < n) {
         seg_push<P>(acc, h, v[m]);
         const uint32_t run_idx = (acc.c & kCountMask) - 1u;
-        const bool last = idx + 1 == n || (m + 1 < N ? ((heads >> (j * N + m + 1)) & 1u) != 0 : next_h != 0);
+        const bool last = (ends >> m) & 1u;
         if (h && keys_out) keys_out[run_idx] = k[m];
         if (last) vals_out[run_idx] = P::out(acc.v);
         if (idx + 1 == n) *num_runs = (unsigned long long)(acc.c & kCountMask);
