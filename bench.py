@@ -968,12 +968,17 @@ def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo
     else:
         reqs_for_baseline = reqs
     per_call = []
+    dev_ms = 0.0  # device time of each plain call alone (CUDA events around it)
+    ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
     for r in reqs_for_baseline:
         a = time.perf_counter()
+        ea.record()
         rc = plain(r)
+        eb.record()
         L.bcx_stream_synchronize(stream)
         per_call.append(time.perf_counter() - a)
+        dev_ms += ea.elapsed_time(eb)
         assert rc == 0
     serial_s = max(time.perf_counter() - t0, 1e-9)
     t0 = time.perf_counter()
@@ -994,6 +999,9 @@ def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo
                             "note": "one plain C-ABI call per request, each waited for"},
            "queued_plain": {"req_per_s": count / queued_s, "GB_per_s": bytes_moved / queued_s / 1e9,
                             "note": "the same plain calls back to back on one stream, one wait at the end"},
+           "kernel_time_bound": {"req_per_s": count / max(dev_ms / 1e3, 1e-9), "device_ms_total": dev_ms,
+                                 "note": "requests over the summed device time of each plain call alone: "
+                                         "the rate of plain kernels with every per-call gap removed"},
            "rates": []}
 
     # -- the server, open-loop Poisson arrivals
@@ -1026,6 +1034,7 @@ def run_serving(torch, bc, dev, count=1000, rates=SERVE_RATES, seed=20261204, lo
     out["server_best_req_per_s"] = best
     out["speedup_vs_serial_plain"] = best / out["serial_plain"]["req_per_s"]
     out["speedup_vs_queued_plain"] = best / out["queued_plain"]["req_per_s"]
+    out["server_vs_kernel_time_bound"] = best / out["kernel_time_bound"]["req_per_s"]
     del arena, pools, vals
     torch.cuda.empty_cache()
     return out

@@ -264,8 +264,25 @@ __device__ __forceinline__ T bcx_warp_fold(T v, int &h) {
   return src.str();
 }
 
-// Elements per thread of the generated kernels: 64 bytes per thread, at
-// most 16 elements.
+// Elements per thread of the generated scan: 128 bytes per thread, at most 32
+// elements.  2^30 int32 on GB300 with the shared-memory transpose and the L2
+// prefetch: 16 per thread 2.94 ms, 24 2.61 ms, 32 2.13 ms (4035 GB/s); the
+// transpose took 32 per thread from 2.64 ms, the prefetch from 2.52 ms.
+inline int jit_scan_items(size_t tsize) {
+  const size_t k = 128 / (tsize ? tsize : 1);
+  return int(k < 1 ? 1 : (k > 32 ? 32 : k));
+}
+// Tiles ahead whose input the generated scan asks L2 to prefetch (16 MB for
+// 32 KB tiles).
+inline int jit_scan_prefetch_tiles() { return 512; }
+// 1: the generated scan reads its tile twice (the second time from L2) and
+// keeps only per-thread totals across the look-back.
+inline int jit_scan_two_read() { return 0; }
+// 1: full aligned tiles move through shared memory (coalesced global access).
+inline int jit_scan_transpose() { return 1; }
+
+// Elements per thread of the generated fold: 64 bytes per thread, at most 16
+// elements.
 inline int jit_items(size_t tsize) {
   const size_t k = 64 / (tsize ? tsize : 1);
   return int(k < 1 ? 1 : (k > 16 ? 16 : k));
@@ -277,12 +294,16 @@ inline int jit_items(size_t tsize) {
 // plain reduce, the transform function applied to a[i] (and b[i]) for a fused
 // transform_reduce, so the transformed values are never written out.
 //
-// One launch: each block folds a contiguous range of 256 x ITEMS element
-// tiles in order (a thread folds its run of ITEMS consecutive elements, a warp
-// folds its threads in lane order, warp 0 folds the warps), writes its
-// partial, and the last block to finish (a ticket taken after a fence) folds
-// the partials in block order with init.  Asynchronous on the queue: its
-// temporaries are stream-ordered and nothing waits for the device.
+// One launch, no block-wide barrier in the main loop: every warp folds its
+// own contiguous range in order, 32 x ITEMS elements at a time (lane l folds
+// its ITEMS consecutive elements -- 16-byte vector loads for a plain read of
+// an aligned array -- then the warp folds its lanes in order); a block folds
+// its eight warps in order and writes its partial, and the last block to
+// finish (a ticket taken after a fence) folds the partials in block order with
+// init.  Asynchronous on the queue: its temporaries are stream-ordered and
+// nothing waits for the device.
+inline bool jit_plain_load(const std::string &load) { return load == "return a[i];"; }
+
 inline std::string jit_fold_source(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                                    const std::string &load, const char *ta, const char *tb) {
   const int items = jit_items(tsize);
@@ -291,46 +312,81 @@ inline std::string jit_fold_source(const std::string &defs, const std::string &o
       << "typedef " << ta << " TA;\n"
       << "typedef " << (tb ? tb : ta) << " TB;\n"
       << "#define BCX_ITEMS " << items << "\n"
+      << "#define BCX_PLAIN_LOAD " << (jit_plain_load(load) ? 1 : 0) << "\n"
       << "__device__ __forceinline__ T bcx_load(const TA *__restrict__ a, const TB *__restrict__ b,"
       << " unsigned long long i) { " << load << " }\n"
       << R"BCX(
+constexpr unsigned long long BCX_CHUNK = 32ull * BCX_ITEMS;
+constexpr bool BCX_VEC_OK = BCX_PLAIN_LOAD && (BCX_ITEMS * sizeof(TA)) % 16 == 0;
+// This lane's ITEMS elements from t0 (all in range when FULL), folded in order.
+template <bool FULL, class TAx = TA>
+__device__ __forceinline__ void bcx_lane_fold(const TAx *__restrict__ a, const TB *__restrict__ b,
+                                              unsigned long long t0, unsigned long long hi, int vec, T &v, int &h) {
+  v = T();
+  h = 0;
+  if constexpr (BCX_VEC_OK && FULL) {
+    if (vec) {
+      constexpr int V = (int)(BCX_ITEMS * sizeof(TA) / 16);
+      uint4 u[V > 0 ? V : 1];
+#pragma unroll
+      for (int j = 0; j < V; ++j) u[j] = __ldcs(reinterpret_cast<const uint4 *>(a + t0) + j);
+      TAx x[BCX_ITEMS];
+      bcx_copy<(sizeof(x) < sizeof(u) ? sizeof(x) : sizeof(u))>(x, u);
+#pragma unroll
+      for (int k = 0; k < BCX_ITEMS; ++k) bcx_comb(v, h, (T)x[k], 1);
+      return;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < BCX_ITEMS; ++k)
+    if (FULL || t0 + k < hi) bcx_comb(v, h, bcx_load(a, b, t0 + k), 1);
+}
+
 extern "C" __global__ void __launch_bounds__(256)
-bcx_jit_fold(const TA *__restrict__ a, const TB *__restrict__ b, unsigned long long n, unsigned long long per_block,
+bcx_jit_fold(const TA *__restrict__ a, const TB *__restrict__ b, unsigned long long n, unsigned long long per_warp,
              T *__restrict__ part, int *__restrict__ part_has, unsigned *__restrict__ done, T init, int has_init,
-             T *__restrict__ out) {
-  constexpr unsigned long long TILE = 256ull * BCX_ITEMS;
+             T *__restrict__ out, int vec) {
   __shared__ __align__(16) unsigned char s_raw[8 * sizeof(T)];
   __shared__ int s_has[8];
   __shared__ bool s_last;
   T *s_val = reinterpret_cast<T *>(s_raw);
   const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const unsigned long long lo = blockIdx.x * per_block;
-  const unsigned long long hi = lo + per_block < n ? lo + per_block : n;
+  const unsigned long long gw = (unsigned long long)blockIdx.x * 8 + warp;
+  const unsigned long long lo = gw * per_warp < n ? gw * per_warp : n;
+  const unsigned long long hi = lo + per_warp < n ? lo + per_warp : n;
   T acc = T();
-  int acc_h = 0;  // meaningful in thread 0
-  for (unsigned long long base = lo; base < hi; base += TILE) {
-    const unsigned long long t0 = base + (unsigned long long)threadIdx.x * BCX_ITEMS;
-    T v = T();
-    int h = 0;
-#pragma unroll
-    for (int k = 0; k < BCX_ITEMS; ++k)
-      if (t0 + k < hi) bcx_comb(v, h, bcx_load(a, b, t0 + k), 1);
-    v = bcx_warp_fold(v, h);
-    if (lane == 0) { s_val[warp] = v; s_has[warp] = h; }
-    __syncthreads();
-    if (warp == 0) {
-      T w = lane < 8 ? s_val[lane] : T();
-      int wh = lane < 8 ? s_has[lane] : 0;
-      w = bcx_warp_fold(w, wh);
-      if (lane == 0) bcx_comb(acc, acc_h, w, wh);
-    }
-    __syncthreads();
+  int acc_h = 0;
+  unsigned long long base = lo;
+  // two chunks per step, so two chunks of loads are in flight
+  for (; base + 2 * BCX_CHUNK <= hi; base += 2 * BCX_CHUNK) {
+    T v0, v1;
+    int h0, h1;
+    bcx_lane_fold<true>(a, b, base + lane * BCX_ITEMS, hi, vec, v0, h0);
+    bcx_lane_fold<true>(a, b, base + BCX_CHUNK + lane * BCX_ITEMS, hi, vec, v1, h1);
+    v0 = bcx_warp_fold(v0, h0);
+    v1 = bcx_warp_fold(v1, h1);
+    bcx_comb(acc, acc_h, v0, h0);
+    bcx_comb(acc, acc_h, v1, h1);
   }
-  if (threadIdx.x == 0) {
-    part[blockIdx.x] = acc;
-    part_has[blockIdx.x] = acc_h;
-    __threadfence();
-    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  for (; base < hi; base += BCX_CHUNK) {
+    T v;
+    int h;
+    bcx_lane_fold<false>(a, b, base + lane * BCX_ITEMS, hi, vec, v, h);
+    v = bcx_warp_fold(v, h);
+    bcx_comb(acc, acc_h, v, h);
+  }
+  if (lane == 0) { s_val[warp] = acc; s_has[warp] = acc_h; }
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < 8 ? s_val[lane] : T();
+    int wh = lane < 8 ? s_has[lane] : 0;
+    w = bcx_warp_fold(w, wh);
+    if (lane == 0) {
+      part[blockIdx.x] = w;
+      part_has[blockIdx.x] = wh;
+      __threadfence();
+      s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
   }
   __syncthreads();
   if (!s_last || warp != 0) return;
@@ -338,8 +394,8 @@ bcx_jit_fold(const TA *__restrict__ a, const TB *__restrict__ b, unsigned long l
   T r = T();
   int rh = 0;
   if (has_init) { r = init; rh = 1; }
-  for (unsigned base = 0; base < gridDim.x; base += 32) {
-    const unsigned i = base + lane;
+  for (unsigned base2 = 0; base2 < gridDim.x; base2 += 32) {
+    const unsigned i = base2 + lane;
     T w = T();
     int wh = 0;
     if (i < gridDim.x) { w = bcx_ldcg(part + i); wh = __ldcg(part_has + i); }
@@ -354,17 +410,22 @@ bcx_jit_fold(const TA *__restrict__ a, const TB *__restrict__ b, unsigned long l
 
 inline void jit_fold(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                      const std::string &load, const char *ta, const char *tb, const void *a, const void *b,
-                     size_t n, const void *init, void *out, command_queue &queue) {
+                     size_t n, const void *init, void *out, command_queue &queue, size_t ta_size = 0) {
   const std::string s = jit_fold_source(defs, op, t, tsize, load, ta, tb);
-  const int items = jit_items(tsize);
-  const size_t tile = size_t(256) * size_t(items);
-  const size_t tiles = (n + tile - 1) / tile;
-  size_t blocks = tiles < 1 ? 1 : tiles;
-  const size_t cap = size_t(sm_count()) * 4;
-  if (blocks > cap) blocks = cap;
-  const size_t tiles_per_block = (tiles + blocks - 1) / blocks;
-  blocks = tiles ? (tiles + tiles_per_block - 1) / tiles_per_block : 1;
-  unsigned long long per_block = (unsigned long long)(tiles_per_block * tile);
+  const size_t items = size_t(jit_items(tsize));
+  const size_t chunk = 32 * items;
+  const size_t chunks = (n + chunk - 1) / chunk;
+  // about 8 blocks of 8 warps per SM, each warp a contiguous range of whole
+  // chunks (at least 4)
+  size_t warps = size_t(sm_count()) * 64;
+  const size_t max_warps = (chunks + 3) / 4;
+  if (warps > max_warps) warps = max_warps;
+  if (warps < 1) warps = 1;
+  const size_t per_warp_chunks = (chunks + warps - 1) / warps;
+  unsigned long long per_warp = (unsigned long long)(per_warp_chunks * chunk);
+  const size_t blocks = ((chunks + per_warp_chunks - 1) / per_warp_chunks + 7) / 8;
+  const size_t tas = ta_size ? ta_size : tsize;
+  int vec = jit_plain_load(load) && (items * tas) % 16 == 0 && reinterpret_cast<uintptr_t>(a) % 16 == 0;
   // partials, their flags and the ticket of the last block, in one temporary
   const size_t part_bytes = (blocks * tsize + 255) & ~size_t(255);
   const size_t has_bytes = (blocks * sizeof(int) + 255) & ~size_t(255);
@@ -378,8 +439,8 @@ inline void jit_fold(const std::string &defs, const std::string &op, const char 
   int has_init = init != nullptr;
   unsigned long long nn = n;
   const void *bb = b ? b : a;
-  void *args[] = {(void *)&a, (void *)&bb, (void *)&nn, (void *)&per_block, (void *)&part, (void *)&part_has,
-                  (void *)&done, (void *)init_bytes.data(), (void *)&has_init, (void *)&out};
+  void *args[] = {(void *)&a, (void *)&bb, (void *)&nn, (void *)&per_warp, (void *)&part, (void *)&part_has,
+                  (void *)&done, (void *)init_bytes.data(), (void *)&has_init, (void *)&out, (void *)&vec};
   jit_launch(s, "bcx_jit_fold", unsigned(blocks), 256, queue, args);
   check(bcx_free_async(tmp, queue.get()));
 }
@@ -451,20 +512,36 @@ inline void jit_reduce(const std::string &defs, const std::string &op, const cha
 
 // Scan with a user functor: one launch of a single-pass decoupled look-back
 // scan (the design of the library's built-in scan, detail/scan_on_gpu.hpp
-// replaced): each block takes the next tile from a ticket, scans its 256 x
-// ITEMS elements in registers (a thread's run, then the warp, then the
-// block), publishes the tile's aggregate, and warp 0 looks back over 32
-// predecessor tiles per step -- bounded waits, reported through the library's
-// error word -- for the exclusive prefix, which every thread folds into its
-// outputs.  Exclusive scans start from init (tile 0 publishes init OP its
-// aggregate).  In place is allowed: every thread reads all of its elements
-// before it writes any.  Asynchronous on the queue: no host waits, and the
-// status array is a stream-ordered temporary.
-inline std::string jit_scan_source(const std::string &defs, const std::string &op, const char *t, size_t tsize) {
-  const int items = jit_items(tsize);
+// replaced): each block takes the next tile from a ticket and asks L2 for the
+// tile prefetch_tiles tickets ahead; full aligned tiles arrive through shared
+// memory (coalesced 16-byte loads, then each thread reads its contiguous run);
+// the tile is scanned in registers (a thread's run, then the warp, then the
+// block), its aggregate published, and warp 0 looks back over 32 predecessor
+// tiles per step (lookback_depth windows polled at once) -- bounded waits,
+// reported through the library's error word -- for the exclusive prefix, which
+// every thread folds into its outputs; outputs leave through shared memory the
+// same way.  Exclusive scans start from init (tile 0 publishes init OP its
+// aggregate).  In place is allowed: a tile is read whole before any of it is
+// written, and no other tile touches it.  Asynchronous on the queue: no host
+// waits, and the status array is a stream-ordered temporary.
+// Tuning knobs (-1 or 0 = default): items per thread, evict-first hints,
+// prefetch distance, two_read (re-read the tile from L2 instead of keeping it
+// in registers across the look-back), look-back depth, transpose.
+inline std::string jit_scan_source(const std::string &defs, const std::string &op, const char *t, size_t tsize,
+                                   int items_override = 0, bool streaming = true, int prefetch_tiles = -1,
+                                   int two_read = -1, int lookback_depth = 1, int transpose = -1) {
+  if (two_read < 0) two_read = jit_scan_two_read();
+  if (transpose < 0) transpose = jit_scan_transpose();
+  const int items = items_override > 0 ? items_override : jit_scan_items(tsize);
+  if (prefetch_tiles < 0) prefetch_tiles = jit_scan_prefetch_tiles();
   const bool packed = tsize <= 4;
   std::ostringstream src;
   src << jit_common(defs, op, t) << "#define BCX_ITEMS " << items << "\n#define BCX_PACKED " << (packed ? 1 : 0)
+      << "\n#define BCX_PREFETCH_TILES " << prefetch_tiles << "\n#define BCX_TWO_READ " << two_read
+      << "\n#define BCX_LOOKBACK_DEPTH " << (lookback_depth > 0 ? lookback_depth : 1)
+      << "\n#define BCX_TRANSPOSE " << ((transpose && (items * tsize) % 16 == 0) ? 1 : 0)
+      << "\n#define BCX_LD(p) " << (streaming ? "__ldcs(p)" : "(*(p))") << "\n#define BCX_ST(p, v) "
+      << (streaming ? "__stcs(p, v)" : "(*(p) = (v))")
       << R"BCX(
 #define BCX_SPIN_LIMIT (1u << 22)
 // Tile status: flag 0 = nothing yet, 1 = aggregate, 2 = inclusive prefix.
@@ -504,48 +581,123 @@ __device__ __forceinline__ unsigned bcx_poll(unsigned long long *, unsigned *fla
 // Warp 0: exclusive prefix of tile `tile` (>= 1) over its predecessors.
 __device__ T bcx_lookback(unsigned long long *words, unsigned *flags, T *agg, T *inc, unsigned long long tile,
                           unsigned *err) {
+  // Each step polls BCX_LOOKBACK_DEPTH windows of 32 predecessors at once (one
+  // L2 round trip), then folds them nearest first up to the nearest prefix.
   const unsigned lane = threadIdx.x & 31u;
   T ex = T();
   int eh = 0;
   long long pred = (long long)tile - 1;
   bool gave_up = false;
   while (true) {
-    const long long t = pred - (long long)lane;
-    T v = T();
-    unsigned f = 2u;  // before tile 0: never reached (tile 0 publishes a prefix)
-    int vh = 0;
-    if (t >= 0) { f = bcx_poll(words, flags, agg, inc, (unsigned long long)t, &v); vh = 1; }
-    unsigned spins = 0;
-    while (true) {
-      const unsigned pmask = __ballot_sync(0xffffffffu, f == 2u);
-      const int first = pmask ? __ffs(pmask) - 1 : 31;
-      const unsigned need = first == 31 ? 0xffffffffu : ((2u << first) - 1u);
-      if (!(__ballot_sync(0xffffffffu, f == 0u) & need)) break;
-      if (++spins > BCX_SPIN_LIMIT) {
-        gave_up = true;
-        if (f == 0u) { f = 2u; vh = 0; }
-        break;
+    T v[BCX_LOOKBACK_DEPTH];
+    unsigned f[BCX_LOOKBACK_DEPTH];
+    int vh[BCX_LOOKBACK_DEPTH];
+#pragma unroll
+    for (int j = 0; j < BCX_LOOKBACK_DEPTH; ++j) {
+      const long long t = pred - (long long)lane - 32ll * j;
+      v[j] = T();
+      f[j] = 2u;  // before tile 0: never reached (tile 0 publishes a prefix)
+      vh[j] = 0;
+      if (t >= 0) { f[j] = bcx_poll(words, flags, agg, inc, (unsigned long long)t, &v[j]); vh[j] = 1; }
+    }
+    bool done = false;
+#pragma unroll
+    for (int j = 0; j < BCX_LOOKBACK_DEPTH; ++j) {
+      if (done) break;
+      const long long t = pred - (long long)lane - 32ll * j;
+      unsigned spins = 0;
+      while (true) {
+        const unsigned pmask = __ballot_sync(0xffffffffu, f[j] == 2u);
+        const int first = pmask ? __ffs(pmask) - 1 : 31;
+        const unsigned need = first == 31 ? 0xffffffffu : ((2u << first) - 1u);
+        if (!(__ballot_sync(0xffffffffu, f[j] == 0u) & need)) break;
+        if (++spins > BCX_SPIN_LIMIT) {
+          gave_up = true;
+          if (f[j] == 0u) { f[j] = 2u; vh[j] = 0; }
+          break;
+        }
+        __nanosleep(spins < 32 ? 32 : 256);
+        if (f[j] == 0u && t >= 0) f[j] = bcx_poll(words, flags, agg, inc, (unsigned long long)t, &v[j]);
       }
-      __nanosleep(spins < 32 ? 32 : 256);
-      if (f == 0u && t >= 0) f = bcx_poll(words, flags, agg, inc, (unsigned long long)t, &v);
+      const unsigned pmask = __ballot_sync(0xffffffffu, f[j] == 2u);
+      const int first = pmask ? __ffs(pmask) - 1 : 31;
+      int wh = ((int)lane <= first) ? vh[j] : 0;
+      // lane order is newest-first: fold from the oldest (highest lane) down
+      const T rv = bcx_shfl_idx(v[j], 31 - (int)lane);
+      int fh = __shfl_sync(0xffffffffu, wh, 31 - (int)lane);
+      const T w = bcx_warp_fold(rv, fh);
+      if (fh) {
+        ex = eh ? bcx_op(w, ex) : w;
+        eh = 1;
+      }
+      done = pmask != 0;
     }
-    const unsigned pmask = __ballot_sync(0xffffffffu, f == 2u);
-    const int first = pmask ? __ffs(pmask) - 1 : 31;
-    int wh = ((int)lane <= first) ? vh : 0;
-    // lane order is newest-first: fold from the oldest (highest lane) down
-    const T rv = bcx_shfl_idx(v, 31 - (int)lane);
-    const int rh = __shfl_sync(0xffffffffu, wh, 31 - (int)lane);
-    int fh = rh;
-    const T w = bcx_warp_fold(rv, fh);
-    if (fh) {
-      ex = eh ? bcx_op(w, ex) : w;
-      eh = 1;
-    }
-    if (pmask) break;
-    pred -= 32;
+    if (done) break;
+    pred -= 32ll * BCX_LOOKBACK_DEPTH;
   }
   if (__any_sync(0xffffffffu, gave_up) && lane == 0 && err) atomicOr(err, 1u);
   return ex;
+}
+
+// This thread's elements t0 .. t0+ITEMS-1 (vector loads for full aligned
+// tiles; `keep` caches the read in L2 for a second read).
+template <bool FULL>
+__device__ __forceinline__ void bcx_scan_load(const T *in, unsigned long long t0, int cnt, int vec,
+                                              T (&x)[BCX_ITEMS], bool keep) {
+  if (FULL && vec) {
+    constexpr int V = (int)(BCX_ITEMS * sizeof(T) / 16);
+    uint4 u[V > 0 ? V : 1];
+#pragma unroll
+    for (int j = 0; j < V; ++j)
+      u[j] = keep ? __ldcg(reinterpret_cast<const uint4 *>(in + t0) + j)
+                  : BCX_LD(reinterpret_cast<const uint4 *>(in + t0) + j);
+    bcx_copy<(sizeof(x) < sizeof(u) ? sizeof(x) : sizeof(u))>(x, u);
+  } else {
+#pragma unroll
+    for (int k = 0; k < BCX_ITEMS; ++k) x[k] = (FULL || k < cnt) ? in[t0 + k] : T();
+  }
+}
+
+// Full aligned tiles moved through shared memory: the warp reads and writes
+// global memory in coalesced 16-byte vectors (lane-consecutive), each thread
+// works on its contiguous run.  One 16-byte pad slot every 8 vectors keeps a
+// thread's run reads free of bank conflicts.
+constexpr int BCX_TVECS = (int)(256ull * BCX_ITEMS * sizeof(T) / 16);
+constexpr int BCX_TV = (int)(BCX_ITEMS * sizeof(T) / 16);  // vectors per thread
+__device__ __forceinline__ int bcx_pad(int i) { return i + (i >> 3); }
+__device__ __forceinline__ uint4 *bcx_tile_smem() {
+  __shared__ uint4 s_tile[BCX_TRANSPOSE ? BCX_TVECS + BCX_TVECS / 8 : 1];
+  return s_tile;
+}
+__device__ __forceinline__ void bcx_transpose_load(const T *in, unsigned long long tile_base, T (&x)[BCX_ITEMS]) {
+  uint4 *sm = bcx_tile_smem();
+  const uint4 *src = reinterpret_cast<const uint4 *>(in + tile_base);
+#pragma unroll
+  for (int j = 0; j < BCX_TV; ++j) {
+    const int i = j * 256 + (int)threadIdx.x;
+    sm[bcx_pad(i)] = BCX_LD(src + i);
+  }
+  __syncthreads();
+  uint4 u[BCX_TV > 0 ? BCX_TV : 1];
+#pragma unroll
+  for (int j = 0; j < BCX_TV; ++j) u[j] = sm[bcx_pad((int)threadIdx.x * BCX_TV + j)];
+  bcx_copy<(sizeof(x) < sizeof(u) ? sizeof(x) : sizeof(u))>(x, u);
+}
+__device__ __forceinline__ void bcx_transpose_store(T *out, unsigned long long tile_base, const T (&y)[BCX_ITEMS]) {
+  uint4 *sm = bcx_tile_smem();
+  uint4 u[BCX_TV > 0 ? BCX_TV : 1];
+  bcx_copy<(sizeof(y) < sizeof(u) ? sizeof(y) : sizeof(u))>(u, y);
+  // every thread has read its own run before the look-back barrier, so the
+  // runs can be overwritten in place
+#pragma unroll
+  for (int j = 0; j < BCX_TV; ++j) sm[bcx_pad((int)threadIdx.x * BCX_TV + j)] = u[j];
+  __syncthreads();
+  uint4 *dst = reinterpret_cast<uint4 *>(out + tile_base);
+#pragma unroll
+  for (int j = 0; j < BCX_TV; ++j) {
+    const int i = j * 256 + (int)threadIdx.x;
+    BCX_ST(dst + i, sm[bcx_pad(i)]);
+  }
 }
 
 template <bool FULL>
@@ -564,21 +716,17 @@ __device__ __forceinline__ void bcx_scan_tile(const T *in, T *out, unsigned long
     cnt = r <= 0 ? 0 : (r < BCX_ITEMS ? (int)r : BCX_ITEMS);
   }
   T x[BCX_ITEMS];
-  if (FULL && vec) {
-    constexpr int V = (int)(BCX_ITEMS * sizeof(T) / 16);
-    uint4 u[V > 0 ? V : 1];
-#pragma unroll
-    for (int j = 0; j < V; ++j) u[j] = __ldcs(reinterpret_cast<const uint4 *>(in + t0) + j);
-    bcx_copy<(sizeof(x) < sizeof(u) ? sizeof(x) : sizeof(u))>(x, u);
-  } else {
-#pragma unroll
-    for (int k = 0; k < BCX_ITEMS; ++k) x[k] = (FULL || k < cnt) ? in[t0 + k] : T();
-  }
-  // this thread's run, inclusive
+  const unsigned long long tile_base = tile * TILE;
+  if (BCX_TRANSPOSE && FULL && vec) bcx_transpose_load(in, tile_base, x);
+  else bcx_scan_load<FULL>(in, t0, cnt, vec, x, BCX_TWO_READ != 0);
+  // this thread's run, inclusive (kept in x unless the tile is read twice)
   T run = x[0];
 #pragma unroll
   for (int k = 1; k < BCX_ITEMS; ++k)
-    if (FULL || k < cnt) { run = bcx_op(run, x[k]); x[k] = run; }
+    if (FULL || k < cnt) {
+      run = bcx_op(run, x[k]);
+      if (!BCX_TWO_READ) x[k] = run;
+    }
   int h = FULL ? 1 : (cnt > 0);
   // lanes of the warp, inclusive
   T a = run;
@@ -618,7 +766,18 @@ __device__ __forceinline__ void bcx_scan_tile(const T *in, T *out, unsigned long
   for (unsigned j = 0; j < warp; ++j) bcx_comb(p, ph, s_val[j], s_has[j]);
   bcx_comb(p, ph, lane_ex, lane_eh);
   T y[BCX_ITEMS];
-  if (exclusive) {
+  if (BCX_TWO_READ) {
+    // second read of the tile (from L2): fold the prefix through the run
+    bcx_scan_load<FULL>(in, t0, cnt, vec, x, false);
+    T r = p;
+    int rh = ph;
+#pragma unroll
+    for (int k = 0; k < BCX_ITEMS; ++k) {
+      if (exclusive) y[k] = rh ? r : T();
+      bcx_comb(r, rh, x[k], 1);
+      if (!exclusive) y[k] = r;
+    }
+  } else if (exclusive) {
     y[0] = ph ? p : T();
 #pragma unroll
     for (int k = 1; k < BCX_ITEMS; ++k) y[k] = ph ? bcx_op(p, x[k - 1]) : x[k - 1];
@@ -626,12 +785,14 @@ __device__ __forceinline__ void bcx_scan_tile(const T *in, T *out, unsigned long
 #pragma unroll
     for (int k = 0; k < BCX_ITEMS; ++k) y[k] = ph ? bcx_op(p, x[k]) : x[k];
   }
-  if (FULL && vec) {
+  if (BCX_TRANSPOSE && FULL && vec) {
+    bcx_transpose_store(out, tile_base, y);
+  } else if (FULL && vec) {
     constexpr int V = (int)(BCX_ITEMS * sizeof(T) / 16);
     uint4 u[V > 0 ? V : 1];
     bcx_copy<(sizeof(y) < sizeof(u) ? sizeof(y) : sizeof(u))>(u, y);
 #pragma unroll
-    for (int j = 0; j < V; ++j) __stcs(reinterpret_cast<uint4 *>(out + t0) + j, u[j]);
+    for (int j = 0; j < V; ++j) BCX_ST(reinterpret_cast<uint4 *>(out + t0) + j, u[j]);
   } else {
 #pragma unroll
     for (int k = 0; k < BCX_ITEMS; ++k)
@@ -646,6 +807,19 @@ bcx_jit_scan(const T *in, T *out, unsigned long long n, unsigned *ticket, unsign
   if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
   __syncthreads();
   const unsigned long long tile = s_tile;
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+  // ask L2 for the tile BCX_PREFETCH_TILES tickets ahead (16-byte aligned
+  // input only, clipped to the array)
+  if (BCX_PREFETCH_TILES > 0 && vec && threadIdx.x == 0) {
+    const unsigned long long f0 = (tile + BCX_PREFETCH_TILES) * (256ull * BCX_ITEMS);
+    if (f0 < n) {
+      const unsigned long long m = n - f0 < 256ull * BCX_ITEMS ? n - f0 : 256ull * BCX_ITEMS;
+      const unsigned bytes = (unsigned)(m * sizeof(T)) & ~15u;
+      if (bytes)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(in + f0), "r"(bytes) : "memory");
+    }
+  }
+#endif
   if (n - tile * (256ull * BCX_ITEMS) >= 256ull * BCX_ITEMS)
     bcx_scan_tile<true>(in, out, n, tile, words, flags, agg, inc, init, has_init, exclusive, vec, err);
   else
@@ -657,10 +831,12 @@ bcx_jit_scan(const T *in, T *out, unsigned long long n, unsigned *ticket, unsign
 
 inline void jit_scan(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                      const void *in, void *out, size_t n, bool exclusive, const void *init,
-                     command_queue &queue) {
+                     command_queue &queue, int items_override = 0, bool streaming = true, int prefetch_tiles = -1,
+                     int two_read = -1, int lookback_depth = 1, int transpose = -1) {
   if (n == 0) return;
-  const std::string s = jit_scan_source(defs, op, t, tsize);
-  const int items = jit_items(tsize);
+  const std::string s = jit_scan_source(defs, op, t, tsize, items_override, streaming, prefetch_tiles, two_read,
+                                        lookback_depth, transpose);
+  const int items = items_override > 0 ? items_override : jit_scan_items(tsize);
   const bool packed = tsize <= 4;
   const size_t tile = size_t(256) * size_t(items);
   const size_t tiles = (n + tile - 1) / tile;
