@@ -49,24 +49,22 @@ using namespace radix;
 
 // ---------------------------------------------------------------------------
 // 1. Histogram of every digit position, one read of the keys.  Keys stream in
-// as 16-byte vectors; a warp whose 32 keys are identical adds 32 once per
-// digit position instead of 32 shared-memory atomics on one address (the
-// all-equal and heavily skewed distributions).
+// as 16-byte vectors; when the 32 lanes' vectors all hold one key (all-equal
+// and heavily skewed distributions), lane 0 adds 32 x N once per digit
+// position instead of 32 x N shared-memory atomics on one address.  PLAIN keys
+// (unsigned, ascending) skip the key transform.
 template <class U, int PASSES>
-__device__ __forceinline__ void hist_count(uint32_t (*sh)[kRadix], U k, bool valid, unsigned lane) {
-  const U k0 = __shfl_sync(0xffffffffu, k, 0);
-  if (__all_sync(0xffffffffu, valid && k == k0)) {
-    if (lane == 0) {
+__device__ __forceinline__ void hist_add(uint32_t (*sh)[kRadix], U k, uint32_t c) {
 #pragma unroll
-      for (int p = 0; p < PASSES; ++p) atomicAdd(&sh[p][uint32_t(k0 >> (p * kRadixBits)) & (kRadix - 1)], 32u);
-    }
-  } else if (valid) {
-#pragma unroll
-    for (int p = 0; p < PASSES; ++p) atomicAdd(&sh[p][uint32_t(k >> (p * kRadixBits)) & (kRadix - 1)], 1u);
-  }
+  for (int p = 0; p < PASSES; ++p) atomicAdd(&sh[p][uint32_t(k >> (p * kRadixBits)) & (kRadix - 1)], c);
 }
 
-template <class U, int PASSES>
+template <class U, int PASSES, bool PLAIN>
+__device__ __forceinline__ U hist_key(U x, const KeyXform<U> &xf) {
+  return PLAIN ? x : apply_xform<U>(x, xf);
+}
+
+template <class U, int PASSES, bool PLAIN>
 __global__ void __launch_bounds__(kHistThreads)
 radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t nvec, const KeyXform<U> xf,
                        uint32_t *__restrict__ hist) {
@@ -80,14 +78,10 @@ radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t
   // Unaligned head and the tail: the first warp, 32 scalars at a time.
   if (warp_id == 0) {
     const size_t tail = head + nvec * N;
-    for (size_t b = 0; b < head; b += kWarp) {
-      const bool valid = b + lane < head;
-      hist_count<U, PASSES>(sh, valid ? apply_xform<U>(keys[b + lane], xf) : U(0), valid, lane);
-    }
-    for (size_t b = tail; b < n; b += kWarp) {
-      const bool valid = b + lane < n;
-      hist_count<U, PASSES>(sh, valid ? apply_xform<U>(keys[b + lane], xf) : U(0), valid, lane);
-    }
+    for (size_t b = 0; b < head; b += kWarp)
+      if (b + lane < head) hist_add<U, PASSES>(sh, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
+    for (size_t b = tail; b < n; b += kWarp)
+      if (b + lane < n) hist_add<U, PASSES>(sh, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
   }
   const vec16<U> *vk = reinterpret_cast<const vec16<U> *>(keys + head);
   for (size_t vb = warp_id * kWarp; vb < nvec; vb += nwarps * kWarp) {
@@ -95,9 +89,16 @@ radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t
     const bool valid = v < nvec;
     vec16<U> r;
     if (valid) r = ld_stream16(vk + v);
+    bool same = valid;
 #pragma unroll
-    for (int j = 0; j < N; ++j)
-      hist_count<U, PASSES>(sh, valid ? apply_xform<U>(r.v[j], xf) : U(0), valid, lane);
+    for (int j = 1; j < N; ++j) same = same && r.v[j] == r.v[0];
+    const U k0 = __shfl_sync(0xffffffffu, r.v[0], 0);
+    if (__all_sync(0xffffffffu, same && r.v[0] == k0)) {
+      if (lane == 0) hist_add<U, PASSES>(sh, hist_key<U, PASSES, PLAIN>(k0, xf), uint32_t(kWarp * N));
+    } else if (valid) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) hist_add<U, PASSES>(sh, hist_key<U, PASSES, PLAIN>(r.v[j], xf), 1u);
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistThreads) {
@@ -302,8 +303,12 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
     size_t cap = size_t(ds->sm_count) * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    radix_histogram_kernel<U, PASSES><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, xf,
-                                                                                 hist);
+    if (kind == kKeyUnsigned && !desc)
+      radix_histogram_kernel<U, PASSES, true><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, xf,
+                                                                                        hist);
+    else
+      radix_histogram_kernel<U, PASSES, false><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, xf,
+                                                                                         hist);
     rc = launch_status("radix_histogram");
     if (rc) return rc;
   }
