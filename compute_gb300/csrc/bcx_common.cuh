@@ -315,6 +315,20 @@ __device__ __forceinline__ void bulk_store_global(void *dst, const void *src, ui
                "r"(bytes)
                : "memory");
 }
+// Per-thread asynchronous copy of BYTES (4, 8 or 16; both addresses aligned to
+// BYTES) from global into shared memory, bypassing registers.  The thread
+// waits for all of its copies with cp_async_wait_all(); a block barrier after
+// that wait makes them visible to the other threads.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_smem(void *dst, const void *src) {
+  static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async moves 4, 8 or 16 bytes");
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(BYTES)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void bulk_commit_group() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_group_read0() {
   asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");

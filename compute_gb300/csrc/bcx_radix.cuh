@@ -15,9 +15,11 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / kWarp;
-// Onesweep blocks resident per SM the register budget is sized for (85
-// registers a thread at 256 threads).
-constexpr int kSortBlocksPerSm = 3;
+// Onesweep blocks resident per SM the register budget is sized for (64
+// registers a thread at 256 threads; 53 KB of shared memory a block with
+// 16-bit counters and uint32 values).  One pass over 2^28 uint32 pairs on
+// GB300: 3 blocks 1.262 ms, 4 blocks 1.236 ms (values copied asynchronously).
+constexpr int kSortBlocksPerSm = 4;
 constexpr int kHistThreads = 256;
 
 // Status word of one (tile, digit) during one digit pass: a tag in the high
@@ -133,12 +135,20 @@ __device__ __forceinline__ uint32_t onesweep_lookback(const unsigned long long *
 // Shared-memory footprint of one onesweep block: per-warp digit counters
 // (later the tile-local start of each warp's run of each digit), then the
 // tile's keys and values staged in digit order.
-template <class U, int VB, int IPT_ = items_per_thread<U>::value>
+// Counter width in bytes: a tile holds at most 65536 keys, so 16-bit counters
+// suffice (and leave room for a fourth block per SM).
+constexpr int kCounterBytes = 2;
+template <int CB> struct counter_type;
+template <> struct counter_type<2> { typedef uint16_t type; };
+template <> struct counter_type<4> { typedef uint32_t type; };
+
+template <class U, int VB, int IPT_ = items_per_thread<U>::value, int CB = kCounterBytes>
 struct OnesweepSmem {
   typedef typename value_type_of<VB>::type VT;
+  typedef typename counter_type<CB>::type CT;
   static constexpr int IPT = IPT_;
   static constexpr int TILE = kSortThreads * IPT;
-  static constexpr size_t kCounters = size_t(kSortWarps) * kRadix * 4;
+  static constexpr size_t kCounters = size_t(kSortWarps) * kRadix * CB;
   static constexpr size_t kKeys = kCounters;
   static constexpr size_t kVals = kKeys + ((size_t(TILE) * sizeof(U) + 15) & ~size_t(15));
   static constexpr size_t kBytes = kVals + (VB ? size_t(TILE) * sizeof(VT) : 0);
@@ -153,7 +163,22 @@ enum RankMethod : int { kRankMatch = 0, kRankMatchAhead = 1, kRankBallot = 2 };
 // update depends on the previous one, so warps stall on it; the ballots are
 // plain ALU work.  One pass over 2^28 uint32 pairs on GB300 (16 keys per
 // thread): kRankMatch 2.10 ms, kRankMatchAhead 2.23 ms, kRankBallot 1.40 ms.
+// With 24 keys per thread, computing the ballots of 4 or 8 items ahead of
+// their counter updates gave the same time (1.233-1.235 ms against 1.236),
+// and counter updates by shared-memory atomics from each digit's lowest lane
+// were slower (1.27 ms): the ballots are limited by issue throughput, not by
+// the counter chain.
 constexpr int kRankDefault = kRankBallot;
+
+// How values reach their digit-order slots in shared memory: kValsRegs loads
+// them into registers before the look-back and stores them after it;
+// kValsAsync copies each value from global memory straight to its slot with
+// cp.async (4-, 8- and 16-byte values), holding no registers across the walk.
+// One pass over 2^28 uint32 pairs on GB300 at 3 blocks per SM: registers
+// 1.262 ms, asynchronous 1.299 ms; at 4 blocks per SM (which the register
+// variant cannot reach without spilling its 24 values) asynchronous 1.236 ms.
+enum ValueStaging : int { kValsRegs = 0, kValsAsync = 1 };
+constexpr int kValsDefault = kValsAsync;
 
 // Lanes of this warp whose digit equals d (d < kRadix for valid lanes;
 // `valid_mask` holds the valid lanes).
@@ -185,15 +210,16 @@ __device__ __forceinline__ uint32_t key_digit(U x, const KeyXform<U> &xf, int sh
 //
 // Order of work: load the keys warp-striped (item i of lane l is element
 // warp_first + 32 i + l, so (i, l) order is input order), rank every key
-// within its warp with one match per item against per-warp digit counters
-// (stable: a key's rank counts the equal digits before it in input order),
-// publish the tile's digit counts, stage keys in shared memory in digit order,
-// issue the value loads, and only then look back over predecessor tiles: by
-// then the predecessors, which started earlier, have mostly published their
-// inclusive prefixes, so the walk is short.  Values are staged once they
-// arrive and the whole tile is written out in digit order, each digit's run to
-// consecutive addresses.
-template <class U, int VB, bool PLAIN, bool FULL, int IPT_, int RANK, int LBW, int PF = 0>
+// within its warp against per-warp digit counters (stable: a key's rank
+// counts the equal digits before it in input order), publish the tile's digit
+// counts, stage keys in shared memory in digit order while the values are
+// copied to their digit-order slots, and only then look back over
+// predecessor tiles: by then the predecessors, which started earlier, have
+// mostly published their inclusive prefixes, so the walk is short.  The whole
+// tile is then written out in digit order, each digit's run to consecutive
+// addresses.
+template <class U, int VB, bool PLAIN, bool FULL, int IPT_, int RANK, int LBW, int PF = 0, int CB = kCounterBytes,
+          int VS = kValsDefault>
 __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, U *__restrict__ dst_k,
                                                    const typename value_type_of<VB>::type *__restrict__ src_v,
                                                    typename value_type_of<VB>::type *__restrict__ dst_v,
@@ -201,13 +227,14 @@ __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, 
                                                    uint32_t first_tile, const uint32_t *__restrict__ digit_start,
                                                    uint32_t dst_limit, int pass, int shift, const KeyXform<U> &xf,
                                                    unsigned long long *__restrict__ status, uint32_t *err) {
-  typedef OnesweepSmem<U, VB, IPT_> L;
+  typedef OnesweepSmem<U, VB, IPT_, CB> L;
   typedef typename L::VT VT;
+  typedef typename L::CT CT;
   constexpr int IPT = L::IPT;
   static_assert(kSortThreads == kRadix, "one thread per digit");
   static_assert(L::TILE <= 65536, "16-bit tile positions");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint32_t *wcnt = reinterpret_cast<uint32_t *>(smem_raw);  // [kSortWarps][kRadix]
+  CT *wcnt = reinterpret_cast<CT *>(smem_raw);               // [kSortWarps][kRadix]
   U *s_keys = reinterpret_cast<U *>(smem_raw + L::kKeys);    // digit order
   VT *s_vals = reinterpret_cast<VT *>(smem_raw + L::kVals);  // digit order
   __shared__ uint32_t s_gofs[kRadix];  // output index of a digit's run minus its tile-local start
@@ -232,9 +259,9 @@ __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, 
     }
   }
   const uint32_t dstart = digit_start[tid];
-  uint32_t *my_cnt = wcnt + warp * kRadix;
+  CT *my_cnt = wcnt + warp * kRadix;
 #pragma unroll
-  for (int j = 0; j < kRadix / kWarp; ++j) my_cnt[j * kWarp + lane] = 0;
+  for (int j = 0; j < kRadix * CB / 4 / kWarp; ++j) reinterpret_cast<uint32_t *>(my_cnt)[j * kWarp + lane] = 0;
   const uint32_t warp_first = warp * (kWarp * IPT);
   const U *wk = src_k + base + warp_first + lane;
   U key[IPT];
@@ -271,7 +298,7 @@ __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, 
     uint32_t prior = 0;
     if (valid) prior = my_cnt[d];
     __syncwarp();
-    if (valid && below == 0) my_cnt[d] = prior + __popc(peers);
+    if (valid && below == 0) my_cnt[d] = CT(prior + __popc(peers));
     __syncwarp();
     if (i & 1) pos[i / 2] |= (prior + below) << 16;
     else pos[i / 2] = prior + below;
@@ -302,13 +329,21 @@ __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, 
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) {
       const uint32_t c = wcnt[w * kRadix + tid];
-      wcnt[w * kRadix + tid] = run;
+      wcnt[w * kRadix + tid] = CT(run);
       run += c;
     }
   }
   __syncthreads();
 
-  // Stage keys in digit order.
+  // Stage keys in digit order.  Values are copied asynchronously to their
+  // slots as each position is known (their latency overlaps the walk, and
+  // they hold no registers); or, for 1- and 2-byte values and the register
+  // variant, values of up to 4 bytes are loaded before the look-back and
+  // staged after it, and wider ones are staged first, in groups, to bound the
+  // registers they hold.
+  const VT *wv = src_v + base + warp_first + lane;
+  constexpr bool kAsync = VB && VS == kValsAsync && sizeof(VT) >= 4;
+  constexpr bool kEarly = !kAsync && sizeof(VT) <= 4;
 #pragma unroll
   for (int i = 0; i < IPT; ++i) {
     if (FULL || warp_first + i * kWarp + lane < count) {
@@ -316,21 +351,19 @@ __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, 
       const uint32_t half = (i & 1) ? 16 : 0;
       const uint32_t p = my_cnt[d] + ((pos[i / 2] >> half) & 0xffffu);
       s_keys[p] = key[i];
-      pos[i / 2] = (pos[i / 2] & (0xffff0000u >> half)) | (p << half);
+      if constexpr (kAsync)
+        cp_async_smem<sizeof(VT)>(s_vals + p, wv + i * kWarp);
+      else
+        pos[i / 2] = (pos[i / 2] & (0xffff0000u >> half)) | (p << half);
     }
   }
-  const VT *wv = src_v + base + warp_first + lane;
-  // Values of up to 4 bytes are loaded before the look-back and staged after
-  // it, so their load latency overlaps the walk; wider values are staged
-  // first, in groups, to bound the registers they hold.
-  constexpr bool kEarly = sizeof(VT) <= 4;
   VT val[(VB && kEarly) ? IPT : 1];
   if (VB && kEarly) {
 #pragma unroll
     for (int i = 0; i < IPT; ++i)
       if (FULL || warp_first + i * kWarp + lane < count) val[i] = wv[i * kWarp];
   }
-  if (VB && !kEarly) {
+  if (VB && !kEarly && !kAsync) {
     constexpr int G = 4;
 #pragma unroll
     for (int g = 0; g < IPT; g += G) {
@@ -362,6 +395,7 @@ __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, 
       if (FULL || warp_first + i * kWarp + lane < count)
         s_vals[(pos[i / 2] >> ((i & 1) ? 16 : 0)) & 0xffffu] = val[i];
   }
+  if (kAsync) cp_async_wait_all();
   __syncthreads();
 
   // Write out: consecutive threads take consecutive digit-order positions.
@@ -390,7 +424,7 @@ __device__ __forceinline__ void onesweep_tile_impl(const U *__restrict__ src_k, 
 // The partial last tile takes a separate, out-of-line copy of the routine so
 // that its bounds checks do not raise the register pressure of the full-tile
 // path.
-template <class U, int VB, bool PLAIN, int IPT, int RANK, int LBW>
+template <class U, int VB, bool PLAIN, int IPT, int RANK, int LBW, int CB, int VS>
 __device__ __noinline__ void onesweep_partial_tile(const U *__restrict__ src_k, U *__restrict__ dst_k,
                                                    const typename value_type_of<VB>::type *__restrict__ src_v,
                                                    typename value_type_of<VB>::type *__restrict__ dst_v,
@@ -398,12 +432,13 @@ __device__ __noinline__ void onesweep_partial_tile(const U *__restrict__ src_k, 
                                                    uint32_t first_tile, const uint32_t *__restrict__ digit_start,
                                                    uint32_t dst_limit, int pass, int shift, const KeyXform<U> xf,
                                                    unsigned long long *__restrict__ status, uint32_t *err) {
-  onesweep_tile_impl<U, VB, PLAIN, false, IPT, RANK, LBW>(src_k, dst_k, src_v, dst_v, base, count, tile, first_tile,
-                                                          digit_start, dst_limit, pass, shift, xf, status, err);
+  onesweep_tile_impl<U, VB, PLAIN, false, IPT, RANK, LBW, 0, CB, VS>(src_k, dst_k, src_v, dst_v, base, count, tile,
+                                                                     first_tile, digit_start, dst_limit, pass, shift,
+                                                                     xf, status, err);
 }
 
 template <class U, int VB, bool PLAIN, int IPT = items_per_thread<U>::value, int RANK = kRankDefault,
-          int LBW = kLookbackWindow, int PF = kOnesweepPrefetchTiles>
+          int LBW = kLookbackWindow, int PF = kOnesweepPrefetchTiles, int CB = kCounterBytes, int VS = kValsDefault>
 __device__ __forceinline__ void onesweep_tile(const U *__restrict__ src_k, U *__restrict__ dst_k,
                                               const typename value_type_of<VB>::type *__restrict__ src_v,
                                               typename value_type_of<VB>::type *__restrict__ dst_v,
@@ -411,13 +446,14 @@ __device__ __forceinline__ void onesweep_tile(const U *__restrict__ src_k, U *__
                                               const uint32_t *__restrict__ digit_start, uint32_t dst_limit,
                                               int pass, int shift, const KeyXform<U> &xf,
                                               unsigned long long *__restrict__ status, uint32_t *err) {
-  if (count == uint32_t(OnesweepSmem<U, VB, IPT>::TILE))
-    onesweep_tile_impl<U, VB, PLAIN, true, IPT, RANK, LBW, PF>(src_k, dst_k, src_v, dst_v, base, count, tile,
-                                                          first_tile, digit_start, dst_limit, pass, shift, xf,
-                                                          status, err);
+  if (count == uint32_t(OnesweepSmem<U, VB, IPT, CB>::TILE))
+    onesweep_tile_impl<U, VB, PLAIN, true, IPT, RANK, LBW, PF, CB, VS>(src_k, dst_k, src_v, dst_v, base, count, tile,
+                                                                       first_tile, digit_start, dst_limit, pass,
+                                                                       shift, xf, status, err);
   else
-    onesweep_partial_tile<U, VB, PLAIN, IPT, RANK, LBW>(src_k, dst_k, src_v, dst_v, base, count, tile, first_tile,
-                                                        digit_start, dst_limit, pass, shift, xf, status, err);
+    onesweep_partial_tile<U, VB, PLAIN, IPT, RANK, LBW, CB, VS>(src_k, dst_k, src_v, dst_v, base, count, tile,
+                                                                first_tile, digit_start, dst_limit, pass, shift, xf,
+                                                                status, err);
 }
 
 

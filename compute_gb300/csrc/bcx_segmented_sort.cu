@@ -216,7 +216,7 @@ segsort_starts_kernel(const unsigned long long *__restrict__ offsets, const uint
 }
 
 template <class U, int VB, bool PLAIN>
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, kSortBlocksPerSm)
 segsort_onesweep_kernel(U *__restrict__ keys_main, U *__restrict__ keys_alt,
                         typename value_type_of<VB>::type *__restrict__ vals_main,
                         typename value_type_of<VB>::type *__restrict__ vals_alt, uint32_t n,
