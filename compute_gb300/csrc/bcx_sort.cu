@@ -107,6 +107,75 @@ radix_histogram_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t
   }
 }
 
+// The same counts with one column of counters per lane: lane l adds to
+// column l of each (pass, digit) row, so the 32 lanes of an atomic always hit
+// 32 different banks whatever their digits (with one shared row per digit,
+// random digits put about 3.5 lanes on the busiest bank and the atomics
+// serialise on it).  One block of kHistLaneThreads per SM holds
+// PASSES * kRadix * 32 counters (128 KB for 32-bit keys); the columns are
+// summed at the end, each warp reading a rotated order so the sums are
+// conflict-free too.  Each lane keeps kHistLaneUnroll 16-byte loads in
+// flight.  sort_by_key of 2^28 uniform uint32 pairs on GB300: 5.36 ms with
+// the shared rows, 5.11 ms with lane columns (the count at the read
+// bandwidth); Zipf(1.1) keys 5.14 -> 4.99 ms.  Keys of up to 4 bytes take this
+// kernel (tunable "radix_sort"/"histogram_lanes", 0 = shared rows); 64-bit
+// keys, whose 8 passes would need 256 KB, keep the shared rows.
+constexpr int kHistLaneThreads = 1024;
+constexpr int kHistLaneUnroll = 4;
+template <int PASSES>
+constexpr size_t hist_lane_smem() {
+  return size_t(PASSES) * kRadix * kWarp * sizeof(uint32_t);
+}
+
+template <class U, int PASSES, bool PLAIN>
+__device__ __forceinline__ void hist_lane_add(uint32_t *col, U k, uint32_t c) {
+#pragma unroll
+  for (int p = 0; p < PASSES; ++p)
+    atomicAdd(col + (p * kRadix + (uint32_t(k >> (p * kRadixBits)) & (kRadix - 1))) * kWarp, c);
+}
+
+template <class U, int PASSES, bool PLAIN>
+__global__ void __launch_bounds__(kHistLaneThreads, 1)
+radix_histogram_lanes_kernel(const U *__restrict__ keys, size_t n, size_t head, size_t nvec, const KeyXform<U> xf,
+                             uint32_t *__restrict__ hist) {
+  constexpr int N = 16 / sizeof(U);
+  extern __shared__ __align__(16) uint32_t shl[];  // [PASSES][kRadix][kWarp]
+  for (int i = threadIdx.x; i < PASSES * kRadix * kWarp; i += kHistLaneThreads) shl[i] = 0;
+  __syncthreads();
+  const unsigned lane = lane_id();
+  uint32_t *col = shl + lane;
+  const size_t warp_id = (size_t(blockIdx.x) * kHistLaneThreads + threadIdx.x) / kWarp;
+  const size_t nwarps = size_t(gridDim.x) * kHistLaneThreads / kWarp;
+  if (warp_id == 0) {
+    const size_t tail = head + nvec * N;
+    for (size_t b = 0; b < head; b += kWarp)
+      if (b + lane < head) hist_lane_add<U, PASSES, PLAIN>(col, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
+    for (size_t b = tail; b < n; b += kWarp)
+      if (b + lane < n) hist_lane_add<U, PASSES, PLAIN>(col, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
+  }
+  const vec16<U> *vk = reinterpret_cast<const vec16<U> *>(keys + head);
+  constexpr size_t kStep = size_t(kWarp) * kHistLaneUnroll;
+  for (size_t vb = warp_id * kStep; vb < nvec; vb += nwarps * kStep) {
+    vec16<U> r[kHistLaneUnroll];
+#pragma unroll
+    for (int u = 0; u < kHistLaneUnroll; ++u)
+      if (vb + u * kWarp + lane < nvec) r[u] = ld_stream16(vk + vb + u * kWarp + lane);
+#pragma unroll
+    for (int u = 0; u < kHistLaneUnroll; ++u)
+      if (vb + u * kWarp + lane < nvec) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) hist_lane_add<U, PASSES, PLAIN>(col, hist_key<U, PASSES, PLAIN>(r[u].v[j], xf), 1u);
+      }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < PASSES * kRadix; i += kHistLaneThreads) {
+    uint32_t c = 0;
+#pragma unroll 8
+    for (int j = 0; j < kWarp; ++j) c += shl[i * kWarp + ((j + i) & (kWarp - 1))];
+    if (c) atomicAdd(&hist[i], c);
+  }
+}
+
 // 2. Digit start offsets per pass, pass skipping and buffer schedule.
 __global__ void __launch_bounds__(kRadix)
 radix_prep_kernel(uint32_t *__restrict__ hist, int passes, uint32_t n,
@@ -299,16 +368,42 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
     size_t head = (a % sizeof(U)) ? n : ((16u - (a & 15u)) & 15u) / sizeof(U);
     if (head > n) head = n;
     const size_t nvec = (n - head) / N;
-    size_t blocks = div_up(nvec, size_t(kHistThreads) * 4);
-    size_t cap = size_t(ds->sm_count) * 8;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    if (kind == kKeyUnsigned && !desc)
-      radix_histogram_kernel<U, PASSES, true><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, xf,
-                                                                                        hist);
-    else
-      radix_histogram_kernel<U, PASSES, false><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, xf,
-                                                                                         hist);
+    bool lanes = false;
+    if constexpr (PASSES <= 4) {
+      if (param_get("radix_sort", "histogram_lanes", 1u) != 0) {
+        lanes = true;
+        constexpr size_t smem = hist_lane_smem<PASSES>();
+        static bool attr_set = false;
+        if (!attr_set) {
+          BCX_CUDA(cudaFuncSetAttribute(radix_histogram_lanes_kernel<U, PASSES, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+          BCX_CUDA(cudaFuncSetAttribute(radix_histogram_lanes_kernel<U, PASSES, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+          attr_set = true;
+        }
+        size_t blocks = div_up(nvec, size_t(kHistLaneThreads) * kHistLaneUnroll);
+        if (blocks > size_t(ds->sm_count)) blocks = size_t(ds->sm_count);
+        if (blocks < 1) blocks = 1;
+        if (kind == kKeyUnsigned && !desc)
+          radix_histogram_lanes_kernel<U, PASSES, true><<<unsigned(blocks), kHistLaneThreads, smem, s>>>(
+              k_main, n, head, nvec, xf, hist);
+        else
+          radix_histogram_lanes_kernel<U, PASSES, false><<<unsigned(blocks), kHistLaneThreads, smem, s>>>(
+              k_main, n, head, nvec, xf, hist);
+      }
+    }
+    if (!lanes) {
+      size_t blocks = div_up(nvec, size_t(kHistThreads) * 4);
+      size_t cap = size_t(ds->sm_count) * 8;
+      if (blocks > cap) blocks = cap;
+      if (blocks < 1) blocks = 1;
+      if (kind == kKeyUnsigned && !desc)
+        radix_histogram_kernel<U, PASSES, true><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec, xf,
+                                                                                          hist);
+      else
+        radix_histogram_kernel<U, PASSES, false><<<unsigned(blocks), kHistThreads, 0, s>>>(k_main, n, head, nvec,
+                                                                                           xf, hist);
+    }
     rc = launch_status("radix_histogram");
     if (rc) return rc;
   }
