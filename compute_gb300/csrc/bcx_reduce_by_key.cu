@@ -249,12 +249,23 @@ __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 // work in the serial per-lane fold and make the warp scans (one per chunk)
 // rare; measured on GB300 with compensated float values, 16 elements per
 // thread in 4-element runs took 1.77x as long.
+//
+// Values are loaded VG at a time (keys whole, so the previous lane's last key
+// is at hand for the first head flag), which keeps fewer registers live, and
+// 4-byte keys and values run 6 blocks per SM.  The workload is latency-bound
+// (per-tile loads and look-back), so resident warps matter most: 10,000
+// segment-id runs over 9.5e8 int keys with compensated float values on GB300,
+// 4 blocks per SM with whole runs 2.97 ms, 6 blocks 2.69 ms, 6 blocks with
+// values 8 at a time 2.59 ms (4 at a time 2.70; 8 blocks per SM spill heavily,
+// 3.8 ms).
 template <class K, class V>
 struct RbkShape {
   static constexpr int W = sizeof(K) > sizeof(V) ? int(sizeof(K)) : int(sizeof(V));
   static constexpr int N = 64 / W;
   static constexpr int CH = 32 / N;
   static constexpr int TILE = kRbkThreads * N * CH;
+  static constexpr int VG = N / 2;
+  static constexpr int BLOCKS_PER_SM = W == 4 ? 6 : 4;
   static_assert(N * CH <= 32, "head flags of a thread fit one 32-bit mask");
 };
 
@@ -280,7 +291,7 @@ __device__ __forceinline__ void load_run(const T *__restrict__ p, size_t e0, siz
 constexpr size_t kRbkPrefetchBytes = kL2PrefetchBytes;
 
 template <class K, class V, class P>
-__global__ void __launch_bounds__(kRbkThreads, 4)
+__global__ void __launch_bounds__(kRbkThreads, RbkShape<K, V>::BLOCKS_PER_SM)
 reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uint32_t n,
                      K *__restrict__ keys_out, V *__restrict__ vals_out,
                      unsigned long long *__restrict__ num_runs, RbStatus<P> st,
@@ -289,6 +300,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   typedef RbkShape<K, V> Sh;
   constexpr int N = Sh::N;
   constexpr int CH = Sh::CH;
+  constexpr int VG = Sh::VG;
   __shared__ S s_warp[kRbkWarps];
   __shared__ S s_prefix;
   __shared__ uint32_t s_tile;
@@ -323,20 +335,24 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
     K k[N];
-    V v[N];
     load_run<K, N>(keys, e0, n, vec_k != 0, k);
-    load_run<V, N>(vals, e0, n, vec_v != 0, v);
     K prev = __shfl_up_sync(0xffffffffu, k[N - 1], 1);
     if (lane == 0) prev = carry_key;
     carry_key = __shfl_sync(0xffffffffu, k[N - 1], kWarp - 1);
     S a = seg_ident<P>();
 #pragma unroll
-    for (int m = 0; m < N; ++m) {
-      const size_t idx = e0 + m;
-      const K p = m > 0 ? k[m - 1] : prev;
-      const bool h = idx < n && (idx == 0 || !keys_equal(p, k[m]));
-      heads |= uint32_t(h) << (j * N + m);
-      if (idx < n) seg_push<P>(a, h, v[m]);
+    for (int g0 = 0; g0 < N; g0 += VG) {
+      V v[VG];
+      load_run<V, VG>(vals, e0 + g0, n, vec_v != 0, v);
+#pragma unroll
+      for (int mm = 0; mm < VG; ++mm) {
+        const int m = g0 + mm;
+        const size_t idx = e0 + m;
+        const K p = m > 0 ? k[m - 1] : prev;
+        const bool h = idx < n && (idx == 0 || !keys_equal(p, k[m]));
+        heads |= uint32_t(h) << (j * N + m);
+        if (idx < n) seg_push<P>(a, h, v[mm]);
+      }
     }
     S x = a;
 #pragma unroll
@@ -442,22 +458,26 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
       ends &= n - e0 >= 32 ? 0xffffffffu : ((1u << (n - e0)) - 1u);
     }
     if (((hj & (keys_out ? kRunMask : 0u)) | ends) == 0) continue;
-    K k[N];
-    V v[N];
-    load_run<K, N>(keys, e0, n, vec_k != 0, k);
-    load_run<V, N>(vals, e0, n, vec_v != 0, v);
     S acc = seg_comb<P>(pre, lane_pre[j]);
 #pragma unroll
-    for (int m = 0; m < N; ++m) {
-      const size_t idx = e0 + m;
-      const bool h = (hj >> m) & 1u;
-      if (idx < n) {
-        seg_push<P>(acc, h, v[m]);
-        const uint32_t run_idx = (acc.c & kCountMask) - 1u;
-        const bool last = (ends >> m) & 1u;
-        if (h && keys_out) keys_out[run_idx] = k[m];
-        if (last) vals_out[run_idx] = P::out(acc.v);
-        if (idx + 1 == n) *num_runs = (unsigned long long)(acc.c & kCountMask);
+    for (int g0 = 0; g0 < N; g0 += VG) {
+      K k[VG];
+      V v[VG];
+      load_run<K, VG>(keys, e0 + g0, n, vec_k != 0, k);
+      load_run<V, VG>(vals, e0 + g0, n, vec_v != 0, v);
+#pragma unroll
+      for (int mm = 0; mm < VG; ++mm) {
+        const int m = g0 + mm;
+        const size_t idx = e0 + m;
+        const bool h = (hj >> m) & 1u;
+        if (idx < n) {
+          seg_push<P>(acc, h, v[mm]);
+          const uint32_t run_idx = (acc.c & kCountMask) - 1u;
+          const bool last = (ends >> m) & 1u;
+          if (h && keys_out) keys_out[run_idx] = k[mm];
+          if (last) vals_out[run_idx] = P::out(acc.v);
+          if (idx + 1 == n) *num_runs = (unsigned long long)(acc.c & kCountMask);
+        }
       }
     }
   }
