@@ -14,7 +14,8 @@
 // owns a run of consecutive elements (vector loads, coalesced across the
 // warp): it derives head flags from the previous key, folds its run serially,
 // and one warp scan per chunk combines the lanes' folds.  Only the head flags
-// and per-chunk prefixes are kept; warps combine through shared memory, the
+// and per-chunk prefixes (those in shared memory) are kept; warps combine
+// through shared memory, the
 // tile with its predecessors by decoupled look-back (order-preserving, bounded
 // waits, self-validating status words where the value allows), and a second
 // read (from L2), by only the lanes whose run holds a run head or a run end,
@@ -257,7 +258,7 @@ __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 // segment-id runs over 9.5e8 int keys with compensated float values on GB300,
 // 4 blocks per SM with whole runs 2.97 ms, 6 blocks 2.69 ms, 6 blocks with
 // values 8 at a time 2.59 ms (4 at a time 2.70; 8 blocks per SM spill heavily,
-// 3.8 ms).
+// 3.8 ms), and 2.52 ms with the lanes' chunk prefixes kept in shared memory.
 template <class K, class V>
 struct RbkShape {
   static constexpr int W = sizeof(K) > sizeof(V) ? int(sizeof(K)) : int(sizeof(V));
@@ -304,6 +305,10 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   __shared__ S s_warp[kRbkWarps];
   __shared__ S s_prefix;
   __shared__ uint32_t s_tile;
+  // Fold of everything before the lane's run in chunk j (within the warp),
+  // kept in shared memory across the look-back rather than in registers;
+  // only the owning thread reads its entry back.
+  __shared__ S s_lane_pre[CH][kRbkThreads];
   const unsigned lane = lane_id(), warp = threadIdx.x / kWarp;
   uint32_t tile = 0;
   if (!single) {
@@ -324,11 +329,11 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   // owns elements chunk_base + l*N .. + N-1, so (j, l, m) is input order.
   const size_t warp_base = size_t(tile) * Sh::TILE + size_t(warp) * (CH * kWarp * N);
 
-  // Pass 1 over the tile: head flags and per-chunk prefixes.  Only those stay
-  // in registers across the look-back; pass 2 reads the keys and values again
-  // (they were read microseconds earlier, so from L2) to emit the results.
+  // Pass 1 over the tile: head flags (in a register) and per-chunk prefixes
+  // (in shared memory).  Only those are kept across the look-back; pass 2
+  // reads the keys and values again (they were read microseconds earlier, so
+  // from L2) to emit the results.
   uint32_t heads = 0;  // bit j*N+m = element (j, m) starts a run
-  S lane_pre[CH];      // fold of everything before the lane's run in chunk j (within the warp)
   S run = seg_ident<P>();
   K carry_key = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);  // key before chunk j
 #pragma unroll
@@ -365,7 +370,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
     S ex;
     ex.c = __shfl_up_sync(0xffffffffu, x.c, 1);
     ex.v = P::shfl_up(x.v, 1);
-    lane_pre[j] = lane == 0 ? run : seg_comb<P>(run, ex);
+    s_lane_pre[j][threadIdx.x] = lane == 0 ? run : seg_comb<P>(run, ex);
     S tot;
     tot.c = __shfl_sync(0xffffffffu, x.c, kWarp - 1);
     tot.v = P::shfl(x.v, kWarp - 1);
@@ -458,7 +463,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
       ends &= n - e0 >= 32 ? 0xffffffffu : ((1u << (n - e0)) - 1u);
     }
     if (((hj & (keys_out ? kRunMask : 0u)) | ends) == 0) continue;
-    S acc = seg_comb<P>(pre, lane_pre[j]);
+    S acc = seg_comb<P>(pre, s_lane_pre[j][threadIdx.x]);
 #pragma unroll
     for (int g0 = 0; g0 < N; g0 += VG) {
       K k[VG];
