@@ -258,7 +258,9 @@ __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 // segment-id runs over 9.5e8 int keys with compensated float values on GB300,
 // 4 blocks per SM with whole runs 2.97 ms, 6 blocks 2.69 ms, 6 blocks with
 // values 8 at a time 2.59 ms (4 at a time 2.70; 8 blocks per SM spill heavily,
-// 3.8 ms), and 2.52 ms with the lanes' chunk prefixes kept in shared memory.
+// 3.8 ms), 2.52 ms with the lanes' chunk prefixes kept in shared memory, and
+// 2.48 ms with the chunk loops rolled (fewer spills; runs of ~4 keys 3.01 ->
+// 2.65 ms).
 template <class K, class V>
 struct RbkShape {
   static constexpr int W = sizeof(K) > sizeof(V) ? int(sizeof(K)) : int(sizeof(V));
@@ -336,7 +338,9 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   uint32_t heads = 0;  // bit j*N+m = element (j, m) starts a run
   S run = seg_ident<P>();
   K carry_key = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);  // key before chunk j
-#pragma unroll
+  // The chunk loops stay rolled: one chunk's registers live at a time keeps
+  // the spills of the 6-blocks-per-SM budget small.
+#pragma unroll 1
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
     K k[N];
@@ -445,7 +449,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   // long runs (segment ids as keys) almost every lane skips both.  The fold
   // order is unchanged, so results are identical.
   constexpr uint32_t kRunMask = N >= 32 ? 0xffffffffu : ((1u << N) - 1u);
-#pragma unroll
+#pragma unroll 1
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
     // head flag of the element after this lane's run in chunk j
