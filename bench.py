@@ -58,7 +58,7 @@ ONESWEEP_BYTES_PER_PAIR = 16
 # DRAM traffic of one onesweep launch per pair: dram__bytes_read.sum +
 # dram__bytes_write.sum of one captured launch at 2^25 pairs, per pair, scaled
 # to the 2^28-pair launch by the pairs it moves.
-ONESWEEP_DRAM_BYTES_PER_PAIR = 507.375872e6 / (1 << 25)
+ONESWEEP_DRAM_BYTES_PER_PAIR = (278.886656e6 + 239.637504e6) / (1 << 25)
 
 
 def peaks():
