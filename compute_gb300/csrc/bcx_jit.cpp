@@ -244,8 +244,15 @@ bcx_status bcx_jit_launch(bcx_jit_kernel kernel, unsigned grid, unsigned block, 
                           bcx_stream stream, void **args) {
   BCX_CHECK(kernel != nullptr, BCX_INVALID_VALUE, "NULL kernel");
   KernelScope ks("jit", (cudaStream_t)stream);
-  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void *>(kernel), dim3(grid), dim3(block), args,
-                                   shared_bytes, (cudaStream_t)stream);
+  cudaError_t e = cudaSuccess;
+  // Dynamic shared memory above the default 48 KB needs the kernel's opt-in
+  // on the current device (cheap, and idempotent).
+  if (shared_bytes > 48 * 1024)
+    e = cudaFuncSetAttribute(reinterpret_cast<const void *>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(shared_bytes));
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(jit shared memory)");
+  e = cudaLaunchKernel(reinterpret_cast<const void *>(kernel), dim3(grid), dim3(block), args, shared_bytes,
+                       (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_status(e, "cudaLaunchKernel(jit)");
   return BCX_SUCCESS;
 }

@@ -99,7 +99,7 @@ inline int sm_count() {
 
 // Compile (or fetch from the program cache) and launch.
 inline void jit_launch(const std::string &source, const char *name, unsigned grid, unsigned block,
-                       command_queue &queue, void **args) {
+                       command_queue &queue, void **args, size_t shared_bytes = 0) {
   bcx_jit_kernel k = nullptr;
   int rc = bcx_jit_get_kernel(source.c_str(), name, "", &k);
   if (rc == BCX_BUILD_PROGRAM_FAILURE) {
@@ -110,7 +110,7 @@ inline void jit_launch(const std::string &source, const char *name, unsigned gri
     throw program_build_failure(rc, log);
   }
   check(rc);
-  check(bcx_jit_launch(k, grid, block, 0, queue.get(), args));
+  check(bcx_jit_launch(k, grid, block, shared_bytes, queue.get(), args));
 }
 
 inline unsigned grid_for(size_t work, unsigned block) {
@@ -280,6 +280,17 @@ inline int jit_scan_prefetch_tiles() { return 512; }
 inline int jit_scan_two_read() { return 0; }
 // 1: full aligned tiles move through shared memory (coalesced global access).
 inline int jit_scan_transpose() { return 1; }
+// Tile bytes of the staged generated scan (whole tiles moved into and out of
+// shared memory by bulk copies), or 0 where it does not apply: the element
+// size must divide 16 (the tile is handled as 16-byte vectors).  64 KB tiles
+// hold three blocks per SM; 8- and 16-byte elements take 96 KB tiles (two per
+// SM): fewer tiles, so fewer of their dearer fenced look-back steps.
+inline int jit_scan_staged_tile_bytes(size_t tsize) {
+  if (tsize == 0 || tsize > 16 || 16 % tsize != 0) return 0;
+  return tsize >= 8 ? 96 * 1024 : 64 * 1024;
+}
+// Bytes ahead of a staged tile whose input is prefetched into L2.
+inline size_t jit_scan_staged_prefetch_bytes() { return size_t(16) << 20; }
 
 // Elements per thread of the generated fold: 64 bytes per thread, at most 16
 // elements.
@@ -527,16 +538,26 @@ inline void jit_reduce(const std::string &defs, const std::string &op, const cha
 // Tuning knobs (-1 or 0 = default): items per thread, evict-first hints,
 // prefetch distance, two_read (re-read the tile from L2 instead of keeping it
 // in registers across the look-back), look-back depth, transpose.
+// staged_tile_bytes > 0 generates the staged kernel bcx_jit_scan_staged
+// (tiles of that many bytes, inputs and outputs 16-byte aligned), else the
+// register-tile kernel bcx_jit_scan.
 inline std::string jit_scan_source(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                                    int items_override = 0, bool streaming = true, int prefetch_tiles = -1,
-                                   int two_read = -1, int lookback_depth = 1, int transpose = -1) {
+                                   int two_read = -1, int lookback_depth = 1, int transpose = -1,
+                                   int staged_tile_bytes = 0) {
   if (two_read < 0) two_read = jit_scan_two_read();
   if (transpose < 0) transpose = jit_scan_transpose();
   const int items = items_override > 0 ? items_override : jit_scan_items(tsize);
-  if (prefetch_tiles < 0) prefetch_tiles = jit_scan_prefetch_tiles();
+  if (prefetch_tiles < 0)
+    prefetch_tiles = staged_tile_bytes > 0 ? int(jit_scan_staged_prefetch_bytes() / size_t(staged_tile_bytes))
+                                           : jit_scan_prefetch_tiles();
   const bool packed = tsize <= 4;
+  const int staged_blocks = staged_tile_bytes > 0 ? (227 * 1024) / (staged_tile_bytes + 1024) : 1;
   std::ostringstream src;
-  src << jit_common(defs, op, t) << "#define BCX_ITEMS " << items << "\n#define BCX_PACKED " << (packed ? 1 : 0)
+  src << jit_common(defs, op, t) << "#define BCX_STAGED " << (staged_tile_bytes > 0 ? 1 : 0)
+      << "\n#define BCX_STAGED_TILE_BYTES " << (staged_tile_bytes > 0 ? staged_tile_bytes : 16)
+      << "\n#define BCX_STAGED_BLOCKS " << (staged_blocks < 8 ? staged_blocks : 8)
+      << "\n#define BCX_ITEMS " << items << "\n#define BCX_PACKED " << (packed ? 1 : 0)
       << "\n#define BCX_PREFETCH_TILES " << prefetch_tiles << "\n#define BCX_TWO_READ " << two_read
       << "\n#define BCX_LOOKBACK_DEPTH " << (lookback_depth > 0 ? lookback_depth : 1)
       << "\n#define BCX_TRANSPOSE " << ((transpose && (items * tsize) % 16 == 0) ? 1 : 0)
@@ -800,6 +821,7 @@ __device__ __forceinline__ void bcx_scan_tile(const T *in, T *out, unsigned long
   }
 }
 
+#if !BCX_STAGED
 extern "C" __global__ void __launch_bounds__(256)
 bcx_jit_scan(const T *in, T *out, unsigned long long n, unsigned *ticket, unsigned long long *words,
              unsigned *flags, T *agg, T *inc, T init, int has_init, int exclusive, int vec, unsigned *err) {
@@ -825,6 +847,266 @@ bcx_jit_scan(const T *in, T *out, unsigned long long n, unsigned *ticket, unsign
   else
     bcx_scan_tile<false>(in, out, n, tile, words, flags, agg, inc, init, has_init, exclusive, vec, err);
 }
+#endif  // !BCX_STAGED
+
+#if BCX_STAGED
+// ---- staged tiles ----------------------------------------------------------
+// One block = one tile of BCX_STAGED_TILE_BYTES, moved into shared memory by
+// bulk copies on an mbarrier (the whole tile in flight at once, no registers
+// held for it) and out again by bulk copies after the scan.  Thread t owns the
+// contiguous run of BCX_SVPT 16-byte vectors from vector t*BCX_SVPT and visits
+// them from vector (t mod BCX_SVPT) on, wrapping around, so the eight threads
+// of each shared-memory phase touch eight different bank groups; the run is
+// still combined in element order (vectors [r, VPT) fold into pa, [0, r) into
+// pb, and the run is pb then pa).  The second pass rewrites the run in place
+// with its outputs.  Every wait is bounded.
+#define BCX_SVPT ((int)(BCX_STAGED_TILE_BYTES / (256 * 16)))
+#define BCX_SN ((int)(16 / sizeof(T)))
+#define BCX_SITEMS (BCX_SVPT * BCX_SN)
+#define BCX_SPIECE 16384u
+__device__ __forceinline__ unsigned bcx_smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool bcx_mbar_wait(unsigned long long *bar) {
+  for (unsigned i = 0; i < BCX_SPIN_LIMIT; ++i) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(bcx_smem_addr(bar))
+                 : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+extern "C" __global__ void __launch_bounds__(256, BCX_STAGED_BLOCKS)
+bcx_jit_scan_staged(const T *in, T *out, unsigned long long n, unsigned *ticket, unsigned long long *words,
+                    unsigned *flags, T *agg, T *inc, T init, int has_init, int exclusive, unsigned *err) {
+  extern __shared__ __align__(128) unsigned char bcx_stage[];
+  uint4 *tv = reinterpret_cast<uint4 *>(bcx_stage);
+  T *te = reinterpret_cast<T *>(bcx_stage);
+  __shared__ unsigned long long s_bar;
+  __shared__ unsigned s_tile;
+  __shared__ __align__(16) unsigned char s_raw[9 * sizeof(T)];
+  __shared__ int s_has[9];
+  T *s_val = reinterpret_cast<T *>(s_raw);  // [0, 8): warp totals; [8]: tile prefix
+  constexpr unsigned long long TILE = 256ull * BCX_SITEMS;
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(ticket, 1u);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bcx_smem_addr(&s_bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const unsigned long long tile = s_tile;
+  const unsigned long long base = tile * TILE;
+  const unsigned cnt = (unsigned)(n - base < TILE ? n - base : TILE);
+  const unsigned bulk = (cnt * (unsigned)sizeof(T)) & ~15u;
+  const unsigned bulk_elems = bulk / (unsigned)sizeof(T);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bcx_smem_addr(&s_bar)), "r"(bulk)
+                 : "memory");
+    const char *src = reinterpret_cast<const char *>(in + base);
+    for (unsigned off = 0; off < bulk; off += BCX_SPIECE) {
+      const unsigned len = bulk - off < BCX_SPIECE ? bulk - off : BCX_SPIECE;
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       bcx_smem_addr(bcx_stage + off)),
+                   "l"(src + off), "r"(len), "r"(bcx_smem_addr(&s_bar))
+                   : "memory");
+    }
+    // ask L2 for the tile BCX_PREFETCH_TILES tickets ahead
+    const unsigned long long f0 = (tile + BCX_PREFETCH_TILES) * TILE;
+    if (BCX_PREFETCH_TILES > 0 && f0 < n) {
+      const unsigned long long m = n - f0 < TILE ? n - f0 : TILE;
+      const unsigned pf = (unsigned)(m * sizeof(T)) & ~15u;
+      const char *ps = reinterpret_cast<const char *>(in + f0);
+      for (unsigned off = 0; off < pf; off += BCX_SPIECE)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(ps + off),
+                     "r"(pf - off < BCX_SPIECE ? pf - off : BCX_SPIECE)
+                     : "memory");
+    }
+  }
+  // the last tile's ragged end (under 16 bytes) comes in by plain loads
+  for (unsigned i = bulk_elems + threadIdx.x; i < cnt; i += 256) te[i] = in[base + i];
+  const bool arrived = bcx_mbar_wait(&s_bar);
+  if (__syncthreads_or(!arrived)) {
+    // leave only after the copies into this block's shared memory are done
+    if (threadIdx.x == 0) {
+      if (err) atomicOr(err, 2u);
+      bcx_mbar_wait(&s_bar);
+    }
+    return;
+  }
+  const unsigned t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  const bool full = cnt == TILE;
+  const unsigned e_first = t * (unsigned)BCX_SITEMS;
+  const int r = (int)(t % (unsigned)BCX_SVPT);
+  // pass 1: the run's total, in element order (a full tile has every
+  // element, so only each part's first element needs no combine)
+  T a = T(), pa = T();
+  int ah = 0, pah = 0;
+  if (full) {
+#pragma unroll
+    for (int k = 0; k < BCX_SVPT; ++k) {
+      int v = k + r;
+      if (v >= BCX_SVPT) v -= BCX_SVPT;
+      const uint4 u = tv[t * BCX_SVPT + v];
+      T x[BCX_SN];
+      bcx_copy<16>(x, &u);
+      if (k == 0) {
+        a = x[0];
+      } else if (v == 0) {
+        pa = a;
+        a = x[0];
+      } else {
+        a = bcx_op(a, x[0]);
+      }
+#pragma unroll
+      for (int m = 1; m < BCX_SN; ++m) a = bcx_op(a, x[m]);
+    }
+    ah = 1;
+    if (r != 0) pah = 1;
+  } else {
+#pragma unroll
+    for (int k = 0; k < BCX_SVPT; ++k) {
+      int v = k + r;
+      if (v >= BCX_SVPT) v -= BCX_SVPT;
+      if (k > 0 && v == 0) {
+        pa = a;
+        pah = ah;
+        a = T();
+        ah = 0;
+      }
+      const uint4 u = tv[t * BCX_SVPT + v];
+      T x[BCX_SN];
+      bcx_copy<16>(x, &u);
+#pragma unroll
+      for (int m = 0; m < BCX_SN; ++m)
+        if (e_first + (unsigned)(v * BCX_SN + m) < cnt) bcx_comb(a, ah, x[m], 1);
+    }
+  }
+  T pb = T();
+  int pbh = 0;
+  if (r == 0) {
+    pa = a;
+    pah = ah;
+  } else {
+    pb = a;
+    pbh = ah;
+  }
+  T run = pb;
+  int h = pbh;
+  bcx_comb(run, h, pa, pah);
+  // lanes of the warp, inclusive
+  T ia = run;
+#pragma unroll
+  for (unsigned d = 1; d < 32; d <<= 1) {
+    const T o = bcx_shfl_up(ia, d);
+    const int oh = __shfl_up_sync(0xffffffffu, h, d);
+    if (lane >= d && oh) { ia = h ? bcx_op(o, ia) : o; h = 1; }
+  }
+  const T lane_ex = bcx_shfl_up(ia, 1);
+  int lane_eh = __shfl_up_sync(0xffffffffu, h, 1);
+  if (lane == 0) lane_eh = 0;
+  if (lane == 31) { s_val[warp] = ia; s_has[warp] = h; }
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < 8 ? s_val[lane] : T();
+    int wh = lane < 8 ? s_has[lane] : 0;
+    const T agg_t = bcx_warp_fold(w, wh);
+    T ex = T();
+    int eh = 0;
+    if (tile == 0) {
+      if (has_init) { ex = init; eh = 1; }
+      const T inc_t = eh ? bcx_op(ex, agg_t) : agg_t;
+      if (lane == 0) bcx_publish(words, flags, agg, inc, 0, 2u, inc_t);
+    } else {
+      if (lane == 0) bcx_publish(words, flags, agg, inc, tile, 1u, agg_t);
+      ex = bcx_lookback(words, flags, agg, inc, tile, err);
+      eh = 1;
+      if (lane == 0) bcx_publish(words, flags, agg, inc, tile, 2u, bcx_op(ex, agg_t));
+    }
+    if (lane == 0) { s_val[8] = ex; s_has[8] = eh; }
+  }
+  __syncthreads();
+  // prefix of this thread's run: tile prefix, earlier warps, earlier lanes
+  T p = s_val[8];
+  int ph = s_has[8];
+  for (unsigned j = 0; j < warp; ++j) bcx_comb(p, ph, s_val[j], s_has[j]);
+  bcx_comb(p, ph, lane_ex, lane_eh);
+  // pass 2: outputs in place, vector r first (its prefix includes [0, r));
+  // with a full tile and a prefix in hand (all but the array's first run
+  // when there is no init) no element needs a flag
+  T rr = p;
+  int rh = ph;
+  bcx_comb(rr, rh, pb, pbh);
+  if (full && ph) {
+#pragma unroll
+    for (int k = 0; k < BCX_SVPT; ++k) {
+      int v = k + r;
+      if (v >= BCX_SVPT) v -= BCX_SVPT;
+      if (k > 0 && v == 0) rr = p;
+      uint4 u = tv[t * BCX_SVPT + v];
+      T x[BCX_SN], y[BCX_SN];
+      bcx_copy<16>(x, &u);
+      if (exclusive) {
+#pragma unroll
+        for (int m = 0; m < BCX_SN; ++m) {
+          y[m] = rr;
+          rr = bcx_op(rr, x[m]);
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < BCX_SN; ++m) {
+          rr = bcx_op(rr, x[m]);
+          y[m] = rr;
+        }
+      }
+      bcx_copy<16>(&u, y);
+      tv[t * BCX_SVPT + v] = u;
+    }
+  } else {
+#pragma unroll
+  for (int k = 0; k < BCX_SVPT; ++k) {
+    int v = k + r;
+    if (v >= BCX_SVPT) v -= BCX_SVPT;
+    if (k > 0 && v == 0) {
+      rr = p;
+      rh = ph;
+    }
+    uint4 u = tv[t * BCX_SVPT + v];
+    T x[BCX_SN], y[BCX_SN];
+    bcx_copy<16>(x, &u);
+#pragma unroll
+    for (int m = 0; m < BCX_SN; ++m) {
+      const bool ok = full || e_first + (unsigned)(v * BCX_SN + m) < cnt;
+      if (exclusive) {
+        y[m] = rh ? rr : T();
+        if (ok) bcx_comb(rr, rh, x[m], 1);
+      } else {
+        if (ok) bcx_comb(rr, rh, x[m], 1);
+        y[m] = rr;
+      }
+    }
+    bcx_copy<16>(&u, y);
+    tv[t * BCX_SVPT + v] = u;
+  }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    char *dst = reinterpret_cast<char *>(out + base);
+    for (unsigned off = 0; off < bulk; off += BCX_SPIECE) {
+      const unsigned len = bulk - off < BCX_SPIECE ? bulk - off : BCX_SPIECE;
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst + off),
+                   "r"(bcx_smem_addr(bcx_stage + off)), "r"(len)
+                   : "memory");
+    }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+  }
+  for (unsigned i = bulk_elems + threadIdx.x; i < cnt; i += 256) out[base + i] = te[i];
+}
+#endif  // BCX_STAGED
 )BCX";
   return src.str();
 }
@@ -832,13 +1114,17 @@ bcx_jit_scan(const T *in, T *out, unsigned long long n, unsigned *ticket, unsign
 inline void jit_scan(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                      const void *in, void *out, size_t n, bool exclusive, const void *init,
                      command_queue &queue, int items_override = 0, bool streaming = true, int prefetch_tiles = -1,
-                     int two_read = -1, int lookback_depth = 1, int transpose = -1) {
+                     int two_read = -1, int lookback_depth = 1, int transpose = -1, int staged = -1) {
   if (n == 0) return;
+  // The staged kernel takes 16-byte aligned input and output whose element
+  // size divides 16; anything else takes the register-tile kernel.
+  const bool aligned = reinterpret_cast<uintptr_t>(in) % 16 == 0 && reinterpret_cast<uintptr_t>(out) % 16 == 0;
+  const int stage_bytes = (staged != 0 && aligned) ? jit_scan_staged_tile_bytes(tsize) : 0;
   const std::string s = jit_scan_source(defs, op, t, tsize, items_override, streaming, prefetch_tiles, two_read,
-                                        lookback_depth, transpose);
+                                        lookback_depth, transpose, stage_bytes);
   const int items = items_override > 0 ? items_override : jit_scan_items(tsize);
   const bool packed = tsize <= 4;
-  const size_t tile = size_t(256) * size_t(items);
+  const size_t tile = stage_bytes > 0 ? size_t(stage_bytes) / tsize : size_t(256) * size_t(items);
   const size_t tiles = (n + tile - 1) / tile;
   // ticket | status words (packed) or flags + aggregates + inclusive prefixes
   const size_t a256 = 255;
@@ -859,13 +1145,19 @@ inline void jit_scan(const std::string &defs, const std::string &op, const char 
   int has_init = exclusive && init != nullptr;
   if (has_init) std::memcpy(init_bytes.data(), init, tsize);
   int ex = exclusive ? 1 : 0;
-  int vec = (items * tsize) % 16 == 0 && reinterpret_cast<uintptr_t>(in) % 16 == 0 &&
-            reinterpret_cast<uintptr_t>(out) % 16 == 0;
+  int vec = (items * tsize) % 16 == 0 && aligned;
   unsigned long long nn = n;
-  void *args[] = {(void *)&in, (void *)&out, (void *)&nn, (void *)&ticket, (void *)&words, (void *)&flags,
-                  (void *)&agg, (void *)&inc, (void *)init_bytes.data(), (void *)&has_init, (void *)&ex,
-                  (void *)&vec, (void *)&err};
-  jit_launch(s, "bcx_jit_scan", unsigned(tiles), 256, queue, args);
+  if (stage_bytes > 0) {
+    void *args[] = {(void *)&in, (void *)&out, (void *)&nn, (void *)&ticket, (void *)&words, (void *)&flags,
+                    (void *)&agg, (void *)&inc, (void *)init_bytes.data(), (void *)&has_init, (void *)&ex,
+                    (void *)&err};
+    jit_launch(s, "bcx_jit_scan_staged", unsigned(tiles), 256, queue, args, size_t(stage_bytes));
+  } else {
+    void *args[] = {(void *)&in, (void *)&out, (void *)&nn, (void *)&ticket, (void *)&words, (void *)&flags,
+                    (void *)&agg, (void *)&inc, (void *)init_bytes.data(), (void *)&has_init, (void *)&ex,
+                    (void *)&vec, (void *)&err};
+    jit_launch(s, "bcx_jit_scan", unsigned(tiles), 256, queue, args);
+  }
   check(bcx_free_async(tmp, queue.get()));
 }
 

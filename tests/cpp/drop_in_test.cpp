@@ -327,6 +327,67 @@ static void jit_large_cases(compute::command_queue &q) {
   CHECK(fold.begin().read(q) == pref[m - 1]);
 }
 
+// The staged generated scan (whole tiles bulk-copied through shared memory)
+// at its edges: 1- and 2-byte elements whose last tile ends in a ragged tail
+// under 16 bytes, 8-byte elements (96 KB tiles), a non-commutative functor,
+// in place, and an input one element off 16-byte alignment (which takes the
+// register-tile kernel instead).
+static void jit_staged_cases(compute::command_queue &q) {
+  std::mt19937 gen(11);
+  {
+    const size_t n = 300001;  // 4.6 tiles of 64 KB, 1-byte tail
+    std::vector<unsigned char> h(n);
+    for (auto &x : h) x = (unsigned char)(gen() & 0xff);
+    BOOST_COMPUTE_FUNCTION(compute::uchar_, bxor, (compute::uchar_ a, compute::uchar_ b), { return (uchar_)(a ^ b); });
+    compute::vector<unsigned char> d(h.begin(), h.end(), q), o(n, q.get_context());
+    compute::inclusive_scan(d.begin(), d.end(), o.begin(), bxor, q);
+    std::vector<unsigned char> ref(n);
+    unsigned char run = 0;
+    for (size_t i = 0; i < n; ++i) ref[i] = run = (unsigned char)(run ^ h[i]);
+    CHECK(to_host(o, q) == ref);
+  }
+  {
+    const size_t n = 777777;  // "last nonzero" is associative, not commutative
+    std::vector<short> h(n);
+    for (auto &x : h) x = (gen() % 5 == 0) ? short(gen() % 2001) - 1000 : short(0);
+    BOOST_COMPUTE_FUNCTION(compute::short_, last_nz, (compute::short_ a, compute::short_ b), { return b != 0 ? b : a; });
+    compute::vector<short> d(h.begin(), h.end(), q);
+    compute::exclusive_scan(d.begin(), d.end(), d.begin(), short(-7), last_nz, q);  // in place
+    std::vector<short> ref(n);
+    short run = -7;
+    for (size_t i = 0; i < n; ++i) {
+      ref[i] = run;
+      if (h[i] != 0) run = h[i];
+    }
+    CHECK(to_host(d, q) == ref);
+  }
+  {
+    const size_t n = 1000003;  // 81.4 tiles of 96 KB, one element in the tail
+    std::vector<int64_t> h(n);
+    for (auto &x : h) x = int64_t(gen() % 2000001) - 1000000;
+    BOOST_COMPUTE_FUNCTION(compute::long_, add_l, (compute::long_ a, compute::long_ b), { return a + b; });
+    compute::vector<int64_t> d(h.begin(), h.end(), q), o(n, q.get_context());
+    compute::exclusive_scan(d.begin(), d.end(), o.begin(), int64_t(-3), add_l, q);
+    std::vector<int64_t> ref(n);
+    int64_t run = -3;
+    for (size_t i = 0; i < n; ++i) {
+      ref[i] = run;
+      run += h[i];
+    }
+    CHECK(to_host(o, q) == ref);
+    // one element off 16-byte alignment: the register-tile kernel
+    compute::inclusive_scan(d.begin() + 1, d.end(), o.begin() + 1, add_l, q);
+    std::vector<int64_t> got = to_host(o, q);
+    run = 0;
+    bool ok = true;
+    for (size_t i = 1; i < n; ++i) {
+      run += h[i];
+      ok = ok && got[i] == run;
+    }
+    CHECK(ok);
+  }
+}
+
 // zip_iterator, mapped_view and accumulate with an init of another type.
 static void zip_view_cases(compute::command_queue &q) {
   // test/test_zip_iterator.cpp:47-105 (distance)
@@ -691,6 +752,7 @@ static int run_all() {
   reduce_by_key_cases(q);
   jit_cases(q);
   jit_large_cases(q);
+  jit_staged_cases(q);
   zip_view_cases(q);
   transform_reduce_cases(q);
   scan_family_cases(q);

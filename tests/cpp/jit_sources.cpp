@@ -29,6 +29,18 @@ int main() {
                                        "add_four(_1, _2)", "int", 4));
   emit("bcx_jit_scan", jit_scan_source("struct P { float x; float y; int z; int w; };\n",
                                        "P{_1.x + _2.x, _2.y, _1.z + _2.z, _2.w}", "P", 16));
+  // the staged scan (bulk-copied tiles) for every element size that divides 16
+  auto staged = [](const std::string &defs, const char *op, const char *t, size_t ts) {
+    emit("bcx_jit_scan_staged", jit_scan_source(defs, op, t, ts, 0, true, -1, -1, 1, -1,
+                                                jit_scan_staged_tile_bytes(ts)));
+  };
+  staged("", "_1 + _2", "int", 4);
+  staged("", "_1 * _2", "long long", 8);
+  staged("", "max(_1, _2)", "float", 4);
+  staged("", "_1 + _2", "double", 8);
+  staged("", "(unsigned char)(_1 ^ _2)", "unsigned char", 1);
+  staged("", "(short)(_1 + _2)", "short", 2);
+  staged("struct P { float x; float y; int z; int w; };\n", "P{_1.x + _2.x, _2.y, _1.z + _2.z, _2.w}", "P", 16);
   emit("bcx_jit_fold", jit_fold_source("", "_1 + _2", "int", 4, "return a[i];", "int", nullptr));
   emit("bcx_jit_fold", jit_fold_source("", "_1 + _2", "float", 4, "return a[i] * b[i];", "float", "float"));
   emit("bcx_jit_fold", jit_fold_source("struct BcxArg { float v; unsigned long long i; };\n",
@@ -66,9 +78,11 @@ int main() {
                      (int)(a2 * b1 + a3 * b3));
   });
   emit("bcx_jit_scan", jit_scan_source(matmul.defs(), matmul.print(), "int4", 16));
+  staged(matmul.defs(), matmul.print().c_str(), "int4", 16);
   emit("bcx_jit_fold", jit_fold_source(matmul.defs(), matmul.print(), "int4", 16, "return a[i];", "int4", nullptr));
   BOOST_COMPUTE_FUNCTION(int, times, (int x, int y), { return x * y; });
   emit("bcx_jit_scan", jit_scan_source(times.defs(), times.print(), "int", 4));
+  staged(times.defs(), times.print().c_str(), "int", 4);
   using compute::_1;
   using compute::_2;
   const float alpha = 2.5f;
