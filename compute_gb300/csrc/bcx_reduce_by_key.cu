@@ -244,12 +244,12 @@ struct RbStatus<P, 2> {
 template <class K>
 __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 
-// Tile shape: every lane owns N consecutive elements per chunk (64 bytes of
-// the wider of key and value: vector loads when aligned), CH chunks per
-// thread, 32 elements per thread in all.  Long per-lane runs keep most of the
-// work in the serial per-lane fold and make the warp scans (one per chunk)
-// rare; measured on GB300 with compensated float values, 16 elements per
-// thread in 4-element runs took 1.77x as long.
+// Tile shape: every lane owns N consecutive elements per chunk (8 elements:
+// 32 bytes of 4-byte keys and values, 64 bytes of 8-byte ones; vector loads
+// when aligned), CH chunks per thread, 32 elements per thread in all.  Long
+// per-lane runs keep most of the work in the serial per-lane fold and the
+// warp scans (one per chunk) few; measured on GB300 with compensated float
+// values, 16 elements per thread in 4-element runs took 1.77x as long.
 //
 // Values are loaded VG at a time (keys whole, so the previous lane's last key
 // is at hand for the first head flag), which keeps fewer registers live, and
@@ -258,17 +258,20 @@ __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 // segment-id runs over 9.5e8 int keys with compensated float values on GB300,
 // 4 blocks per SM with whole runs 2.97 ms, 6 blocks 2.69 ms, 6 blocks with
 // values 8 at a time 2.59 ms (4 at a time 2.70; 8 blocks per SM spill heavily,
-// 3.8 ms), 2.52 ms with the lanes' chunk prefixes kept in shared memory, and
+// 3.8 ms), 2.52 ms with the lanes' chunk prefixes kept in shared memory,
 // 2.48 ms with the chunk loops rolled (fewer spills; runs of ~4 keys 3.01 ->
-// 2.65 ms).
+// 2.65 ms), and 2.31 ms with 8-element lane runs (4 chunks a thread, 32
+// registers: 8 blocks per SM; runs of ~4 keys 2.38 ms).  Without its
+// look-back the same kernel takes 1.39 ms: the waits for predecessor tiles,
+// which resident blocks cover, are what remain.
 template <class K, class V>
 struct RbkShape {
   static constexpr int W = sizeof(K) > sizeof(V) ? int(sizeof(K)) : int(sizeof(V));
-  static constexpr int N = 64 / W;
+  static constexpr int N = W == 4 ? 8 : 64 / W;
   static constexpr int CH = 32 / N;
   static constexpr int TILE = kRbkThreads * N * CH;
   static constexpr int VG = N / 2;
-  static constexpr int BLOCKS_PER_SM = W == 4 ? 6 : 4;
+  static constexpr int BLOCKS_PER_SM = W == 4 ? 8 : 4;
   static_assert(N * CH <= 32, "head flags of a thread fit one 32-bit mask");
 };
 
