@@ -246,7 +246,7 @@ __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 
 // Tile shape: every lane owns N consecutive elements per chunk (8 elements:
 // 32 bytes of 4-byte keys and values, 64 bytes of 8-byte ones; vector loads
-// when aligned), CH chunks per thread, 32 elements per thread in all.  Long
+// when aligned), CH chunks per thread, EPT elements per thread in all.  Long
 // per-lane runs keep most of the work in the serial per-lane fold and the
 // warp scans (one per chunk) few; measured on GB300 with compensated float
 // values, 16 elements per thread in 4-element runs took 1.77x as long.
@@ -262,17 +262,21 @@ __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 // 2.48 ms with the chunk loops rolled (fewer spills; runs of ~4 keys 3.01 ->
 // 2.65 ms), and 2.31 ms with 8-element lane runs (4 chunks a thread, 32
 // registers: 8 blocks per SM; runs of ~4 keys 2.38 ms).  Without its
-// look-back the same kernel takes 1.39 ms: the waits for predecessor tiles,
-// which resident blocks cover, are what remain.
+// look-back that kernel took 1.39 ms: the waits for predecessor tiles are
+// what remain, so 4-byte keys and values take 64 elements per thread (tiles
+// of 16384, half the look-backs per element): 2.16 ms (runs of ~4 keys
+// 2.19 ms).
 template <class K, class V>
 struct RbkShape {
   static constexpr int W = sizeof(K) > sizeof(V) ? int(sizeof(K)) : int(sizeof(V));
   static constexpr int N = W == 4 ? 8 : 64 / W;
-  static constexpr int CH = 32 / N;
+  static constexpr int EPT = W == 4 ? 64 : 32;  // elements per thread
+  static constexpr int CH = EPT / N;
   static constexpr int TILE = kRbkThreads * N * CH;
   static constexpr int VG = N / 2;
   static constexpr int BLOCKS_PER_SM = W == 4 ? 8 : 4;
-  static_assert(N * CH <= 32, "head flags of a thread fit one 32-bit mask");
+  typedef typename std::conditional<(N * CH > 32), unsigned long long, uint32_t>::type HeadMask;
+  static_assert(N * CH <= 64, "head flags of a thread fit one 64-bit mask");
 };
 
 template <class T, int N>
@@ -338,7 +342,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   // (in shared memory).  Only those are kept across the look-back; pass 2
   // reads the keys and values again (they were read microseconds earlier, so
   // from L2) to emit the results.
-  uint32_t heads = 0;  // bit j*N+m = element (j, m) starts a run
+  typename Sh::HeadMask heads = 0;  // bit j*N+m = element (j, m) starts a run
   S run = seg_ident<P>();
   K carry_key = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);  // key before chunk j
   // The chunk loops stay rolled: one chunk's registers live at a time keeps
@@ -362,7 +366,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
         const size_t idx = e0 + m;
         const K p = m > 0 ? k[m - 1] : prev;
         const bool h = idx < n && (idx == 0 || !keys_equal(p, k[m]));
-        heads |= uint32_t(h) << (j * N + m);
+        heads |= typename Sh::HeadMask(h) << (j * N + m);
         if (idx < n) seg_push<P>(a, h, v[mm]);
       }
     }
@@ -456,11 +460,12 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;
     // head flag of the element after this lane's run in chunk j
-    const uint32_t h_next_lane = __shfl_down_sync(0xffffffffu, heads >> (j * N), 1) & 1u;
-    const uint32_t h_next_chunk = __shfl_sync(0xffffffffu, heads >> (j + 1 < CH ? (j + 1) * N : 0), 0) & 1u;
+    const uint32_t h_next_lane = uint32_t(__shfl_down_sync(0xffffffffu, heads >> (j * N), 1)) & 1u;
+    const uint32_t h_next_chunk =
+        uint32_t(__shfl_sync(0xffffffffu, heads >> (j + 1 < CH ? (j + 1) * N : 0), 0)) & 1u;
     uint32_t next_h = h_next_lane;
     if (lane == kWarp - 1) next_h = j + 1 < CH ? h_next_chunk : uint32_t(after_head);
-    const uint32_t hj = (heads >> (j * N)) & kRunMask;
+    const uint32_t hj = uint32_t(heads >> (j * N)) & kRunMask;
     // run ends: the next element is a head, or the element is the last one
     uint32_t ends = (hj >> 1) | (next_h << (N - 1));
     if (e0 >= n) {
