@@ -506,12 +506,35 @@ def run_e2e(torch, bc, rank, world):
         hv.copy_(dv, non_blocking=True)
         torch.cuda.synchronize()
         copies.append((t1 - t0, time.perf_counter() - t1))
+    # The same plain copies over as many steps as the timed loop, with the
+    # same host refill between steps: the steps that take far longer than
+    # the median occur here too, without any library code in them.
+    plain = []
+    for _ in range(e2e_steps):
+        hk.copy_(src_k)
+        hv.copy_(src_v)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dk.copy_(hk, non_blocking=True)
+        dv.copy_(hv, non_blocking=True)
+        hk.copy_(dk, non_blocking=True)
+        hv.copy_(dv, non_blocking=True)
+        torch.cuda.synchronize()
+        plain.append(time.perf_counter() - t0)
     del dk, dv
     h2d = min(c[0] for c in copies)
     d2h = min(c[1] for c in copies)
+
+    def slow(xs):
+        med = statistics.median(xs)
+        return sum(1 for x in xs if x > 1.5 * med)
+
     link = {"h2d_ms": h2d * 1e3, "d2h_ms": d2h * 1e3, "h2d_GBps": 8 * N_SORT / h2d / 1e9,
             "d2h_GBps": 8 * N_SORT / d2h / 1e9, "copies_ms": (h2d + d2h) * 1e3,
-            "how": "the step's 2 x 4 B x n bytes each way as plain pinned torch copies, best of 3"}
+            "how": "the step's 2 x 4 B x n bytes each way as plain pinned torch copies, best of 3",
+            "plain_copy_steps_ms": [round(x * 1e3, 2) for x in plain],
+            "slow_steps": {"e2e": slow(per), "plain_copies": slow(plain),
+                           "note": "steps over 1.5x their loop's median"}}
     return {"value": job_throughput(N_SORT * e2e_steps, tot, world), "unit": "Gkeys/s", "link_bound": link,
             "h2d_bytes_per_step": 8 * N_SORT, "d2h_bytes_per_step": 8 * N_SORT,
             "ms_per_step": tot / e2e_steps * 1e3, "ms_median_step": statistics.median(per) * 1e3,
