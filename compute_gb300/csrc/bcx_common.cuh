@@ -289,12 +289,12 @@ __device__ __forceinline__ void bulk_load_smem(void *dst, const void *src, uint3
 __device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
-// Distance, in input bytes, at which the two-read tiled kernels (segmented
-// scan, reduce_by_key) ask L2 to prefetch the tile they will reach later: far
-// enough that the prefetch has landed when that tile's block starts, near
-// enough that it is still in L2 then.  Measured on GB300 at 2^28 elements:
-// 8 MB took reduce_by_key 1.28 -> 1.22 ms and segmented scan 0.51 -> 0.49 ms;
-// 32 MB was slower than none.
+// Distance, in input bytes, at which the two-read tiled segmented scan asks
+// L2 to prefetch the tile it will reach later: far enough that the prefetch
+// has landed when that tile's block starts, near enough that it is still in
+// L2 then.  Measured on GB300 at 2^28 elements: 8 MB took the segmented scan
+// 0.51 -> 0.49 ms; 32 MB was slower than none.  (reduce_by_key, with far more
+// input in flight, keeps a shorter distance of its own.)
 constexpr size_t kL2PrefetchBytes = size_t(8) << 20;
 // Asks L2 to prefetch elements [first, first + count) of p, clipped to n.
 // p + first must be 16-byte aligned.
