@@ -363,8 +363,9 @@ segmented_scan_kernel(const T *__restrict__ in, T *__restrict__ out, size_t n,
 template <class T, class P>
 __global__ void __launch_bounds__(kSegThreads)
 segmented_reduce_kernel(const T *__restrict__ in, const unsigned long long *__restrict__ offsets, size_t nseg,
-                        typename P::Acc init, T *__restrict__ out, uint32_t *__restrict__ seg_counter) {
+                        typename P::Acc init, T *__restrict__ out, uint32_t *__restrict__ seg_counter, int vec) {
   typedef typename P::Acc Acc;
+  constexpr int N = 16 / int(sizeof(T));
   __shared__ Acc s_acc[kSegWarps];
   __shared__ uint32_t s_seg;
   while (true) {
@@ -374,15 +375,35 @@ segmented_reduce_kernel(const T *__restrict__ in, const unsigned long long *__re
     if (seg >= nseg) break;
     const size_t b = offsets[seg], e = offsets[seg + 1];
     Acc a0 = P::ident(), a1 = P::ident(), a2 = P::ident(), a3 = P::ident();
-    size_t i = b + threadIdx.x;
-    for (; i + 3 * kSegThreads < e; i += 4 * kSegThreads) {
-      const T x0 = in[i], x1 = in[i + kSegThreads], x2 = in[i + 2 * kSegThreads], x3 = in[i + 3 * kSegThreads];
-      a0 = P::comb(a0, P::from(x0));
-      a1 = P::comb(a1, P::from(x1));
-      a2 = P::comb(a2, P::from(x2));
-      a3 = P::comb(a3, P::from(x3));
+    // Scalar head up to the first 16-byte boundary, then 16-byte vectors,
+    // four in flight per thread, then the scalar tail (the operators are
+    // commutative, so the order of the partial folds is free).
+    size_t hb = e;
+    if (vec) {
+      hb = b + ((16u - (reinterpret_cast<uintptr_t>(in + b) & 15u)) & 15u) / sizeof(T);
+      if (hb > e) hb = e;
     }
-    for (; i < e; i += kSegThreads) a0 = P::comb(a0, P::from(in[i]));
+    for (size_t i = b + threadIdx.x; i < hb; i += kSegThreads) a0 = P::comb(a0, P::from(in[i]));
+    const size_t nvec = (e - hb) / N;
+    const vec16<T> *vp = reinterpret_cast<const vec16<T> *>(in + hb);
+    size_t v = threadIdx.x;
+    for (; v + 3 * kSegThreads < nvec; v += 4 * kSegThreads) {
+      const vec16<T> x0 = ld_stream16(vp + v), x1 = ld_stream16(vp + v + kSegThreads),
+                     x2 = ld_stream16(vp + v + 2 * kSegThreads), x3 = ld_stream16(vp + v + 3 * kSegThreads);
+#pragma unroll
+      for (int m = 0; m < N; ++m) {
+        a0 = P::comb(a0, P::from(x0.v[m]));
+        a1 = P::comb(a1, P::from(x1.v[m]));
+        a2 = P::comb(a2, P::from(x2.v[m]));
+        a3 = P::comb(a3, P::from(x3.v[m]));
+      }
+    }
+    for (; v < nvec; v += kSegThreads) {
+      const vec16<T> x = ld_stream16(vp + v);
+#pragma unroll
+      for (int m = 0; m < N; ++m) a1 = P::comb(a1, P::from(x.v[m]));
+    }
+    for (size_t i = hb + nvec * N + threadIdx.x; i < e; i += kSegThreads) a2 = P::comb(a2, P::from(in[i]));
     Acc a = P::comb(P::comb(a0, a1), P::comb(a2, a3));
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) a = P::comb(a, P::shfl_down(a, d));
@@ -482,7 +503,7 @@ bcx_status run_segmented_reduce(cudaStream_t s, bcx_dtype type, const void *in, 
   KernelScope ks("segmented_reduce", s);
   segmented_reduce_kernel<T, P><<<unsigned(blocks), kSegThreads, 0, s>>>(
       static_cast<const T *>(in), offsets, nseg, P::from_host(init_v), static_cast<T *>(out),
-      static_cast<uint32_t *>(ts.ptr()));
+      static_cast<uint32_t *>(ts.ptr()), reinterpret_cast<uintptr_t>(in) % sizeof(T) == 0 ? 1 : 0);
   return launch_status("segmented_reduce");
 }
 
