@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <atomic>
 #include <string>
 
 #include "bcx.h"
@@ -43,6 +44,11 @@ struct DeviceState {
 };
 // State of the current device (created on first use).
 bcx_status current_device_state(DeviceState **out);
+
+// Opts `kernel` into `bytes` of dynamic shared memory (needed above 48 KB)
+// on the current device, once per device: `done` keeps one bit per device
+// already opted in, one mask per kernel.
+cudaError_t smem_optin(const void *kernel, int bytes, std::atomic<uint64_t> *done);
 
 size_t dtype_size(bcx_dtype t);
 bool dtype_valid(int t);

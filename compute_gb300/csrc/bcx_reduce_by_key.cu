@@ -14,16 +14,15 @@
 // owns a run of consecutive elements (vector loads, coalesced across the
 // warp): it derives head flags from the previous key, folds its run serially,
 // and one warp scan per chunk combines the lanes' folds.  Only the head flags
-// and per-chunk prefixes (those in shared memory) are kept; warps combine
-// through shared memory, the
-// tile with its predecessors by decoupled look-back (order-preserving, bounded
-// waits, self-validating status words where the value allows), and a second
-// read (from L2), by only the lanes whose run holds a run head or a run end,
-// emits the results: run heads write the output key, run ends the reduced
-// value, and the block holding the last element writes the run count --
-// nothing is read back to the host.  Key equality is
-// the typed == of equal_to<T>.  Float plus with compensated=1 carries
-// Neumaier (s, c) pairs.
+// and the per-chunk prefixes (in shared memory) are kept; warps combine
+// through shared memory, the tile with its predecessors by decoupled
+// look-back (order-preserving, bounded waits, self-validating status words
+// where the value allows), and a second read (from L2), by only the lanes
+// whose run holds a run head or a run end, emits the results: run heads write
+// the output key, run ends the reduced value, and the block holding the last
+// element writes the run count -- nothing is read back to the host.  Key
+// equality is the typed == of equal_to<T>.  Float plus with compensated=1
+// carries Neumaier (s, c) pairs.
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -253,7 +252,7 @@ __device__ __forceinline__ bool keys_equal(K a, K b) { return a == b; }
 //
 // Values are loaded VG at a time (keys whole, so the previous lane's last key
 // is at hand for the first head flag), which keeps fewer registers live, and
-// 4-byte keys and values run 6 blocks per SM.  The workload is latency-bound
+// 4-byte keys and values run 8 blocks per SM.  The workload is latency-bound
 // (per-tile loads and look-back), so resident warps matter most: 10,000
 // segment-id runs over 9.5e8 int keys with compensated float values on GB300,
 // 4 blocks per SM with whole runs 2.97 ms, 6 blocks 2.69 ms, 6 blocks with
@@ -351,7 +350,7 @@ reduce_by_key_kernel(const K *__restrict__ keys, const V *__restrict__ vals, uin
   S run = seg_ident<P>();
   K carry_key = (warp_base > 0 && warp_base - 1 < n) ? keys[warp_base - 1] : K(0);  // key before chunk j
   // The chunk loops stay rolled: one chunk's registers live at a time keeps
-  // the spills of the 6-blocks-per-SM budget small.
+  // the spills of the 32-register (8 blocks per SM) budget small.
 #pragma unroll 1
   for (int j = 0; j < CH; ++j) {
     const size_t e0 = warp_base + size_t(j) * kWarp * N + lane * N;

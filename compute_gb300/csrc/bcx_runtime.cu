@@ -45,6 +45,17 @@ bcx_status cuda_status(cudaError_t e, const char *what) {
 static std::mutex g_dev_mu;
 static std::map<int, DeviceState *> g_devices;
 
+cudaError_t smem_optin(const void *kernel, int bytes, std::atomic<uint64_t> *done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = dev < 64 ? (uint64_t(1) << dev) : 0;
+  if (bit && (done->load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done->fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
+
 bcx_status current_device_state(DeviceState **out) {
   int dev = 0;
   BCX_CUDA(cudaGetDevice(&dev));

@@ -423,10 +423,10 @@ bcx_status launch_small(cudaStream_t s, U *k_main, typename value_type_of<VB>::t
     return BCX_UNSUPPORTED;
   } else {
     constexpr size_t smem = SmallTile<U, VB, CAP>::kBytes;
-    static int resident = 0;  // blocks per SM at this shared-memory size
+    static std::atomic<uint64_t> optin{0};
+    BCX_CUDA(smem_optin(reinterpret_cast<const void *>(segsort_small_kernel<U, VB, CAP>), int(smem), &optin));
+    static int resident = 0;  // blocks per SM at this shared-memory size (same GPU model on every device)
     if (!resident) {
-      BCX_CUDA(cudaFuncSetAttribute(segsort_small_kernel<U, VB, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    int(smem)));
       int r = 0;
       BCX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, segsort_small_kernel<U, VB, CAP>, kSortThreads,
                                                              smem));
@@ -450,12 +450,8 @@ bcx_status seg_onesweep_passes(cudaStream_t s, const SegLayout &L, U *k_main, U 
                                const uint32_t *tile_seg, uint32_t *err) {
   constexpr int PASSES = int(sizeof(U));
   constexpr size_t smem = OnesweepSmem<U, VB>::kBytes;
-  static bool attr = false;
-  if (!attr) {
-    BCX_CUDA(cudaFuncSetAttribute(segsort_onesweep_kernel<U, VB, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(smem)));
-    attr = true;
-  }
+  static std::atomic<uint64_t> optin{0};
+  BCX_CUDA(smem_optin(reinterpret_cast<const void *>(segsort_onesweep_kernel<U, VB, PLAIN>), int(smem), &optin));
   for (int p = 0; p < PASSES; ++p) {
     KernelScope ks("segsort_onesweep", s);
     segsort_onesweep_kernel<U, VB, PLAIN><<<L.max_tiles, kSortThreads, smem, s>>>(

@@ -127,7 +127,7 @@ constexpr size_t hist_lane_smem() {
   return size_t(PASSES) * kRadix * kWarp * sizeof(uint32_t);
 }
 
-template <class U, int PASSES, bool PLAIN>
+template <class U, int PASSES>
 __device__ __forceinline__ void hist_lane_add(uint32_t *col, U k, uint32_t c) {
 #pragma unroll
   for (int p = 0; p < PASSES; ++p)
@@ -149,9 +149,9 @@ radix_histogram_lanes_kernel(const U *__restrict__ keys, size_t n, size_t head, 
   if (warp_id == 0) {
     const size_t tail = head + nvec * N;
     for (size_t b = 0; b < head; b += kWarp)
-      if (b + lane < head) hist_lane_add<U, PASSES, PLAIN>(col, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
+      if (b + lane < head) hist_lane_add<U, PASSES>(col, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
     for (size_t b = tail; b < n; b += kWarp)
-      if (b + lane < n) hist_lane_add<U, PASSES, PLAIN>(col, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
+      if (b + lane < n) hist_lane_add<U, PASSES>(col, hist_key<U, PASSES, PLAIN>(keys[b + lane], xf), 1u);
   }
   const vec16<U> *vk = reinterpret_cast<const vec16<U> *>(keys + head);
   constexpr size_t kStep = size_t(kWarp) * kHistLaneUnroll;
@@ -164,7 +164,7 @@ radix_histogram_lanes_kernel(const U *__restrict__ keys, size_t n, size_t head, 
     for (int u = 0; u < kHistLaneUnroll; ++u)
       if (vb + u * kWarp + lane < nvec) {
 #pragma unroll
-        for (int j = 0; j < N; ++j) hist_lane_add<U, PASSES, PLAIN>(col, hist_key<U, PASSES, PLAIN>(r[u].v[j], xf), 1u);
+        for (int j = 0; j < N; ++j) hist_lane_add<U, PASSES>(col, hist_key<U, PASSES, PLAIN>(r[u].v[j], xf), 1u);
       }
   }
   __syncthreads();
@@ -319,12 +319,8 @@ bcx_status onesweep_passes(cudaStream_t s, const SortLayout &L, U *k_main, U *k_
                            size_t n, const KeyXform<U> &xf, const uint32_t *hist, unsigned long long *status,
                            uint32_t *counters, const SortControl *ctrl, uint32_t *err) {
   const size_t smem = OnesweepSmem<U, VB>::kBytes;
-  static bool attr_set = false;
-  if (!attr_set) {
-    BCX_CUDA(cudaFuncSetAttribute(radix_onesweep_kernel<U, VB, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(smem)));
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> optin{0};
+  BCX_CUDA(smem_optin(reinterpret_cast<const void *>(radix_onesweep_kernel<U, VB, PLAIN>), int(smem), &optin));
   for (int p = 0; p < int(sizeof(U)); ++p) {
     KernelScope ks("radix_onesweep", s);
     radix_onesweep_kernel<U, VB, PLAIN><<<L.tiles, kSortThreads, smem, s>>>(
@@ -373,14 +369,11 @@ bcx_status radix_sort_t(cudaStream_t s, void *keys, void *values, size_t n, int 
       if (param_get("radix_sort", "histogram_lanes", 1u) != 0) {
         lanes = true;
         constexpr size_t smem = hist_lane_smem<PASSES>();
-        static bool attr_set = false;
-        if (!attr_set) {
-          BCX_CUDA(cudaFuncSetAttribute(radix_histogram_lanes_kernel<U, PASSES, true>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-          BCX_CUDA(cudaFuncSetAttribute(radix_histogram_lanes_kernel<U, PASSES, false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-          attr_set = true;
-        }
+        static std::atomic<uint64_t> optin_plain{0}, optin_xf{0};
+        BCX_CUDA(smem_optin(reinterpret_cast<const void *>(radix_histogram_lanes_kernel<U, PASSES, true>),
+                            int(smem), &optin_plain));
+        BCX_CUDA(smem_optin(reinterpret_cast<const void *>(radix_histogram_lanes_kernel<U, PASSES, false>),
+                            int(smem), &optin_xf));
         size_t blocks = div_up(nvec, size_t(kHistLaneThreads) * kHistLaneUnroll);
         if (blocks > size_t(ds->sm_count)) blocks = size_t(ds->sm_count);
         if (blocks < 1) blocks = 1;
