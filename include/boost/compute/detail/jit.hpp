@@ -524,23 +524,25 @@ inline void jit_reduce(const std::string &defs, const std::string &op, const cha
 // Scan with a user functor: one launch of a single-pass decoupled look-back
 // scan (the design of the library's built-in scan, detail/scan_on_gpu.hpp
 // replaced): each block takes the next tile from a ticket and asks L2 for the
-// tile prefetch_tiles tickets ahead; full aligned tiles arrive through shared
-// memory (coalesced 16-byte loads, then each thread reads its contiguous run);
-// the tile is scanned in registers (a thread's run, then the warp, then the
-// block), its aggregate published, and warp 0 looks back over 32 predecessor
-// tiles per step (lookback_depth windows polled at once) -- bounded waits,
-// reported through the library's error word -- for the exclusive prefix, which
-// every thread folds into its outputs; outputs leave through shared memory the
-// same way.  Exclusive scans start from init (tile 0 publishes init OP its
-// aggregate).  In place is allowed: a tile is read whole before any of it is
-// written, and no other tile touches it.  Asynchronous on the queue: no host
-// waits, and the status array is a stream-ordered temporary.
-// Tuning knobs (-1 or 0 = default): items per thread, evict-first hints,
-// prefetch distance, two_read (re-read the tile from L2 instead of keeping it
-// in registers across the look-back), look-back depth, transpose.
-// staged_tile_bytes > 0 generates the staged kernel bcx_jit_scan_staged
-// (tiles of that many bytes, inputs and outputs 16-byte aligned), else the
-// register-tile kernel bcx_jit_scan.
+// tile prefetch_tiles tickets ahead.  With 16-byte aligned input and output
+// and an element size that divides 16, the staged kernel moves each whole
+// tile into shared memory by bulk copies and back out the same way (the
+// built-in scan's design); otherwise register tiles are used, full aligned
+// ones arriving through a shared-memory transpose (coalesced 16-byte loads,
+// then each thread reads its contiguous run).  Either way the tile is scanned
+// a thread's run, then the warp, then the block at a time, its aggregate
+// published, and warp 0 looks back over 32 predecessor tiles per step
+// (lookback_depth windows polled at once) -- bounded waits, reported through
+// the library's error word -- for the exclusive prefix, which every thread
+// folds into its outputs.  Exclusive scans start from init (tile 0 publishes
+// init OP its aggregate).  In place is allowed: a tile is read whole before
+// any of it is written, and no other tile touches it.  Asynchronous on the
+// queue: no host waits, and the status array is a stream-ordered temporary.
+// Tuning knobs of the register-tile kernel (-1 or 0 = default): items per
+// thread, evict-first hints, prefetch distance, two_read (re-read the tile
+// from L2 instead of keeping it in registers across the look-back), look-back
+// depth, transpose.  staged_tile_bytes > 0 generates the staged kernel
+// bcx_jit_scan_staged (tiles of that many bytes), else bcx_jit_scan.
 inline std::string jit_scan_source(const std::string &defs, const std::string &op, const char *t, size_t tsize,
                                    int items_override = 0, bool streaming = true, int prefetch_tiles = -1,
                                    int two_read = -1, int lookback_depth = 1, int transpose = -1,
