@@ -289,13 +289,15 @@ __device__ __forceinline__ void bulk_load_smem(void *dst, const void *src, uint3
 __device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
-// Distance, in input bytes, at which the two-read tiled segmented scan asks
-// L2 to prefetch the tile it will reach later: far enough that the prefetch
-// has landed when that tile's block starts, near enough that it is still in
-// L2 then.  Measured on GB300 at 2^28 elements: 8 MB took the segmented scan
-// 0.51 -> 0.49 ms; 32 MB was slower than none.  (reduce_by_key, with far more
-// input in flight, keeps a shorter distance of its own.)
-constexpr size_t kL2PrefetchBytes = size_t(8) << 20;
+// Distance, in input bytes, at which the two-read tiled kernels (segmented
+// scan, reduce_by_key) ask L2 to prefetch the tile they will reach later: far
+// enough that the prefetch has landed when that tile's block starts, near
+// enough that it is still in L2 then -- with tens of MB of input already in
+// flight across the resident blocks, a short distance.  Measured on GB300
+// over 9.5e8 elements in 10,000 segments: segmented scan 1.66 ms at 8 MB,
+// 1.62 ms at 1 MB; reduce_by_key 2.16 ms at 8 MB, 2.11 ms at 1 MB, 2.22 ms at
+// 16 MB, 2.15 ms without prefetch.
+constexpr size_t kL2PrefetchBytes = size_t(1) << 20;
 // Asks L2 to prefetch elements [first, first + count) of p, clipped to n.
 // p + first must be 16-byte aligned.
 template <class T>

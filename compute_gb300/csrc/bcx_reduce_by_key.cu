@@ -300,9 +300,8 @@ __device__ __forceinline__ void load_run(const T *__restrict__ p, size_t e0, siz
 // Bytes ahead of a tile whose keys and values are prefetched into L2.  At 8
 // blocks per SM of 128 KB tiles about 155 MB of input is in flight, more than
 // L2 holds, so a short distance keeps prefetched lines from being evicted
-// before their tile reads them: 10,000 segment-id runs on GB300, 8 MB ahead
-// 2.16 ms, 1 MB 2.11 ms, 16 MB 2.22 ms, none 2.15 ms.
-constexpr size_t kRbkPrefetchBytes = size_t(1) << 20;
+// before their tile reads them.
+constexpr size_t kRbkPrefetchBytes = kL2PrefetchBytes;
 
 template <class K, class V, class P>
 __global__ void __launch_bounds__(kRbkThreads, RbkShape<K, V>::BLOCKS_PER_SM)
